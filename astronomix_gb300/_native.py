@@ -1,0 +1,234 @@
+"""ctypes binding of the C ABI declared in include/amx.h.
+
+The library is loaded from ``_lib/libamx.so`` inside this package.  There is
+no CPU or eager fallback: if the library is missing, every call raises.
+"""
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libamx.so")
+
+# ---- error bits (include/amx.h)
+AMX_OK = 0
+AMX_ERR_INVALID_ARG = 1 << 0
+AMX_ERR_CUDA = 1 << 1
+AMX_ERR_NAN = 1 << 2
+AMX_ERR_NEGATIVE = 1 << 3
+AMX_ERR_NOT_CONVERGED = 1 << 4
+AMX_ERR_TIMEOUT = 1 << 5
+AMX_ERR_BOUNDS = 1 << 6
+AMX_ERR_UNSUPPORTED = 1 << 7
+AMX_ERR_TOO_LARGE = 1 << 8
+
+_ERR_NAMES = {
+    AMX_ERR_INVALID_ARG: "invalid argument",
+    AMX_ERR_CUDA: "CUDA runtime error",
+    AMX_ERR_NAN: "non-finite value",
+    AMX_ERR_NEGATIVE: "negative density or pressure",
+    AMX_ERR_NOT_CONVERGED: "magnetic fixed point hit the iteration cap",
+    AMX_ERR_TIMEOUT: "grid barrier timed out",
+    AMX_ERR_BOUNDS: "index check failed",
+    AMX_ERR_UNSUPPORTED: "configuration not supported by the kernels",
+    AMX_ERR_TOO_LARGE: "size above a fixed limit",
+}
+
+AMX_F32, AMX_F64 = 0, 1
+
+
+class AmxError(RuntimeError):
+    def __init__(self, code, what=""):
+        self.code = code
+        names = [n for b, n in _ERR_NAMES.items() if code & b]
+        super().__init__("%s: %s (code %d)" % (what or "amx", ", ".join(names) or "unknown", code))
+
+
+class amx_config(ctypes.Structure):
+    _fields_ = [
+        ("solver_mode", ctypes.c_int32),
+        ("dtype", ctypes.c_int32),
+        ("dimensionality", ctypes.c_int32),
+        ("num_cells", ctypes.c_int32),
+        ("num_vars", ctypes.c_int32),
+        ("mhd", ctypes.c_int32),
+        ("riemann_solver", ctypes.c_int32),
+        ("limiter", ctypes.c_int32),
+        ("fv_magnetic_integrator", ctypes.c_int32),
+        ("numerical_precision", ctypes.c_int32),
+        ("boundary_handling", ctypes.c_int32),
+        ("bc_lo", ctypes.c_int32 * 3),
+        ("bc_hi", ctypes.c_int32 * 3),
+        ("enforce_positivity", ctypes.c_int32),
+        ("exact_end_time", ctypes.c_int32),
+        ("fixed_timestep", ctypes.c_int32),
+        ("num_timesteps", ctypes.c_int32),
+        ("box_size", ctypes.c_double),
+        ("grid_spacing", ctypes.c_double),
+    ]
+
+
+class amx_params(ctypes.Structure):
+    _fields_ = [
+        ("C_cfl", ctypes.c_double),
+        ("gamma", ctypes.c_double),
+        ("minimum_density", ctypes.c_double),
+        ("minimum_pressure", ctypes.c_double),
+        ("dt_max", ctypes.c_double),
+        ("t_end", ctypes.c_double),
+    ]
+
+
+class amx_run_info(ctypes.Structure):
+    _fields_ = [
+        ("t", ctypes.c_double),
+        ("last_dt", ctypes.c_double),
+        ("steps", ctypes.c_int64),
+        ("magnetic_iterations", ctypes.c_int64),
+        ("last_magnetic_iterations", ctypes.c_int32),
+        ("status", ctypes.c_int32),
+    ]
+
+
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+
+# name -> (restype, argtypes); the complete list of exports of include/amx.h
+SIGNATURES = {
+    "amx_plan_create": (_I32, [ctypes.POINTER(amx_config), _I64, ctypes.POINTER(_P)]),
+    "amx_plan_destroy": (_I32, [_P]),
+    "amx_plan_workspace_bytes": (_I32, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    "amx_plan_reset": (_I32, [_P, _P]),
+    "amx_plan_set_time": (_I32, [_P, _D, _P]),
+    "amx_cfl_dt": (_I32, [_P, _P, ctypes.POINTER(amx_params), ctypes.POINTER(_D), _P]),
+    "amx_fv_hydro_rk2": (_I32, [_P, _P, ctypes.POINTER(amx_params), _D, _P]),
+    "amx_fv_magnetic_update": (_I32, [_P, _P, ctypes.POINTER(amx_params), _D, _P]),
+    "amx_evolve_state": (_I32, [_P, _P, ctypes.POINTER(amx_params), _D, _P]),
+    "amx_run": (_I32, [_P, _P, ctypes.POINTER(amx_params), _I64, ctypes.POINTER(amx_run_info), _P]),
+    "amx_run_until": (_I32, [_P, _P, ctypes.POINTER(amx_params), _I64, _D, ctypes.POINTER(amx_run_info), _P]),
+    "amx_run_async": (_I32, [_P, _P, ctypes.POINTER(amx_params), _I64, _P]),
+    "amx_history": (_I32, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I32), _I64, _P]),
+    "amx_conservation_sums": (_I32, [_P, _P, ctypes.POINTER(amx_params), ctypes.POINTER(_D), _P]),
+    "amx_status": (_I32, [_P, ctypes.POINTER(_I32), _I32, _P]),
+    "amx_version": (ctypes.c_char_p, []),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                "libamx.so not found at %s: build it with `python -m astronomix_gb300._build` "
+                "(there is no CPU fallback)" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code, what=""):
+    if code:
+        raise AmxError(code, what)
+
+
+def make_params(params) -> amx_params:
+    return amx_params(
+        C_cfl=float(params.C_cfl),
+        gamma=float(params.gamma),
+        minimum_density=float(params.minimum_density),
+        minimum_pressure=float(params.minimum_pressure),
+        dt_max=float(params.dt_max),
+        t_end=float(params.t_end),
+    )
+
+
+class Plan:
+    """Owns an ``amx_plan`` (device workspace for one configuration)."""
+
+    def __init__(self, cfg: amx_config, max_history: int = 0):
+        self._L = lib()
+        self.cfg = cfg
+        self.max_history = int(max_history)
+        h = ctypes.c_void_p()
+        check(self._L.amx_plan_create(ctypes.byref(cfg), self.max_history, ctypes.byref(h)), "amx_plan_create")
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self._L.amx_plan_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def workspace_bytes(self) -> int:
+        n = ctypes.c_size_t()
+        check(self._L.amx_plan_workspace_bytes(self.handle, ctypes.byref(n)))
+        return n.value
+
+    def reset(self, stream=0):
+        check(self._L.amx_plan_reset(self.handle, _P(stream)), "amx_plan_reset")
+
+    def set_time(self, t, stream=0):
+        check(self._L.amx_plan_set_time(self.handle, float(t), _P(stream)), "amx_plan_set_time")
+
+    def cfl_dt(self, state_ptr, prm: amx_params, stream=0) -> float:
+        dt = ctypes.c_double()
+        check(self._L.amx_cfl_dt(self.handle, _P(state_ptr), ctypes.byref(prm), ctypes.byref(dt), _P(stream)),
+              "amx_cfl_dt")
+        return dt.value
+
+    def hydro_rk2(self, state_ptr, prm, dt, stream=0):
+        check(self._L.amx_fv_hydro_rk2(self.handle, _P(state_ptr), ctypes.byref(prm), float(dt), _P(stream)),
+              "amx_fv_hydro_rk2")
+
+    def magnetic_update(self, state_ptr, prm, dt, stream=0):
+        check(self._L.amx_fv_magnetic_update(self.handle, _P(state_ptr), ctypes.byref(prm), float(dt),
+                                             _P(stream)), "amx_fv_magnetic_update")
+
+    def evolve(self, state_ptr, prm, dt, stream=0):
+        check(self._L.amx_evolve_state(self.handle, _P(state_ptr), ctypes.byref(prm), float(dt), _P(stream)),
+              "amx_evolve_state")
+
+    def run(self, state_ptr, prm, max_steps, stream=0) -> amx_run_info:
+        info = amx_run_info()
+        check(self._L.amx_run(self.handle, _P(state_ptr), ctypes.byref(prm), int(max_steps), ctypes.byref(info),
+                              _P(stream)), "amx_run")
+        return info
+
+    def run_until(self, state_ptr, prm, max_steps, t_pause, stream=0) -> amx_run_info:
+        info = amx_run_info()
+        check(self._L.amx_run_until(self.handle, _P(state_ptr), ctypes.byref(prm), int(max_steps), float(t_pause),
+                                    ctypes.byref(info), _P(stream)), "amx_run_until")
+        return info
+
+    def run_async(self, state_ptr, prm, max_steps, stream=0):
+        check(self._L.amx_run_async(self.handle, _P(state_ptr), ctypes.byref(prm), int(max_steps), _P(stream)),
+              "amx_run_async")
+
+    def history(self, n, stream=0):
+        dts = (ctypes.c_double * n)()
+        its = (ctypes.c_int32 * n)()
+        check(self._L.amx_history(self.handle, dts, its, int(n), _P(stream)), "amx_history")
+        return list(dts), list(its)
+
+    def conservation_sums(self, state_ptr, prm, stream=0):
+        out = (ctypes.c_double * 5)()
+        check(self._L.amx_conservation_sums(self.handle, _P(state_ptr), ctypes.byref(prm), out, _P(stream)),
+              "amx_conservation_sums")
+        return list(out)
+
+    def status(self, clear=False, stream=0) -> int:
+        st = ctypes.c_int32()
+        check(self._L.amx_status(self.handle, ctypes.byref(st), int(bool(clear)), _P(stream)), "amx_status")
+        return st.value

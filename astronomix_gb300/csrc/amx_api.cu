@@ -1,0 +1,432 @@
+// C-ABI implementation: plans, workspace and launches (host code).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "../../include/amx.h"
+#include "amx_common.cuh"
+#include "fd_api.h"
+#include "fv_kernels.cuh"
+#include "fv_registry.h"
+
+extern "C" int amx_diag_sums_raw(const amx_config* cfg, const void* state, double gamma, double* out_dev,
+                                 void* stream);
+
+using amx::FVControl;
+using amx::FVKernelInfo;
+
+struct amx_plan {
+  amx_config cfg;
+  int device = 0;
+  int num_sms = 0;
+  size_t elem = 4;          // bytes per value
+  long long ncells = 0;
+  size_t ws_bytes = 0;
+  unsigned char* ws = nullptr;
+  // FV
+  void* p1 = nullptr;
+  void* mag0 = nullptr;
+  void* mag1 = nullptr;
+  FVControl* ctl = nullptr;
+  double* dt_hist = nullptr;
+  int* it_hist = nullptr;
+  int64_t max_hist = 0;
+  FVKernelInfo fv{};
+  int fv_grid = 0;
+  double* diag = nullptr;   // 8 doubles of reduction scratch for amx_conservation_sums
+  // FD
+  amx::FDPlan* fd = nullptr;
+};
+
+namespace {
+
+inline int cuda_ok(cudaError_t e) { return e == cudaSuccess ? AMX_OK : AMX_ERR_CUDA; }
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int validate(const amx_config* c) {
+  if (!c) return AMX_ERR_INVALID_ARG;
+  if (c->dtype != AMX_F32 && c->dtype != AMX_F64) return AMX_ERR_INVALID_ARG;
+  if (c->dimensionality < 1 || c->dimensionality > 3) return AMX_ERR_INVALID_ARG;
+  if (c->num_cells < 4) return AMX_ERR_INVALID_ARG;
+  if (!(c->grid_spacing > 0.0)) return AMX_ERR_INVALID_ARG;
+  if (c->solver_mode == AMX_FINITE_VOLUME) {
+    const int nv = c->dimensionality + 2 + (c->mhd ? 3 : 0);
+    if (c->num_vars != nv) return AMX_ERR_INVALID_ARG;
+    if (c->mhd && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
+    if (c->riemann_solver < AMX_HLL || c->riemann_solver > AMX_LAX_FRIEDRICHS) return AMX_ERR_UNSUPPORTED;
+    if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA) return AMX_ERR_UNSUPPORTED;
+    if (c->boundary_handling == AMX_GHOST_CELLS) {
+      for (int k = 0; k < c->dimensionality; ++k) {
+        for (int side = 0; side < 2; ++side) {
+          const int b = side ? c->bc_hi[k] : c->bc_lo[k];
+          if (b != AMX_BC_OPEN && b != AMX_BC_PERIODIC && b != AMX_BC_REFLECTIVE) return AMX_ERR_UNSUPPORTED;
+          // reflective magnetic/velocity fills of the reference flip the wrong
+          // component for 3-vectors; MHD runs are limited to open / periodic
+          if (c->mhd && b == AMX_BC_REFLECTIVE) return AMX_ERR_UNSUPPORTED;
+        }
+        // periodic must be set on both sides (boundaries.py:105-111)
+        if ((c->bc_lo[k] == AMX_BC_PERIODIC) != (c->bc_hi[k] == AMX_BC_PERIODIC)) return AMX_ERR_UNSUPPORTED;
+      }
+    }
+    return AMX_OK;
+  }
+  if (c->solver_mode == AMX_FINITE_DIFFERENCE) {
+    if (c->dimensionality != 3 || !c->mhd) return AMX_ERR_UNSUPPORTED;
+    if (c->num_vars != 11) return AMX_ERR_INVALID_ARG;
+    if (c->num_cells < 8) return AMX_ERR_INVALID_ARG;
+    return AMX_OK;
+  }
+  return AMX_ERR_INVALID_ARG;
+}
+
+long long ipow(long long b, int e) {
+  long long r = 1;
+  while (e-- > 0) r *= b;
+  return r;
+}
+
+template <typename T>
+amx::FVArgs<T> make_fv_args(amx_plan* p, void* state, const amx_params* prm, int mode) {
+  amx::FVArgs<T> a{};
+  const amx_config& c = p->cfg;
+  a.state = static_cast<T*>(state);
+  a.p1 = static_cast<T*>(p->p1);
+  a.mag0 = static_cast<T*>(p->mag0);
+  a.mag1 = static_cast<T*>(p->mag1);
+  a.ctl = p->ctl;
+  a.dt_hist = p->dt_hist;
+  a.it_hist = p->it_hist;
+  a.max_hist = p->max_hist;
+  a.n = c.num_cells;
+  a.ncells = p->ncells;
+  for (int k = 0; k < 3; ++k) a.bc[k] = amx::AxisBC{c.bc_lo[k], c.bc_hi[k]};
+  a.periodic_roll = (c.boundary_handling == AMX_PERIODIC_ROLL);
+  a.limiter = c.limiter;
+  a.integrator = c.fv_magnetic_integrator;
+  a.lm = (c.riemann_solver == AMX_HLLC_LM);
+  a.exact_end_time = c.exact_end_time;
+  a.fixed_timestep = c.fixed_timestep;
+  a.mode = mode;
+  a.dx = c.grid_spacing;
+  a.gamma = prm->gamma;
+  a.C_cfl = prm->C_cfl;
+  a.t_end = prm->t_end;
+  a.dt_fixed = c.num_timesteps > 0 ? prm->t_end / c.num_timesteps : 0.0;
+  a.dt_in = 0.0;
+  a.dt_scale = 1.0;
+  a.tol = (c.numerical_precision == 1) ? 1e-10 : 1e-5;
+  a.max_iters = 1000;
+  a.max_steps = 0;
+  a.t_pause = INFINITY;
+  return a;
+}
+
+// zero the reduction slots and the barrier before a cooperative launch
+int fv_prepare(amx_plan* p, cudaStream_t s) {
+  // cfl, alpha and mag slots are the leading members of FVControl
+  const size_t n = offsetof(FVControl, dt);
+  int rc = cuda_ok(cudaMemsetAsync(p->ctl, 0, n, s));
+  rc |= cuda_ok(cudaMemsetAsync(&p->ctl->bar_count, 0, sizeof(unsigned int) * 2 + sizeof(int), s));
+  return rc;
+}
+
+template <typename T>
+int fv_launch(amx_plan* p, amx::FVArgs<T>& a, cudaStream_t s) {
+  int rc = fv_prepare(p, s);
+  if (rc) return rc;
+  void* args[] = {&a};
+  cudaError_t e = cudaLaunchCooperativeKernel(p->fv.fn, dim3(p->fv_grid), dim3(amx::kFVThreads), args,
+                                              p->fv.smem, s);
+  return cuda_ok(e);
+}
+
+int fv_run_mode(amx_plan* p, void* state, const amx_params* prm, int mode, double dt_in, double dt_scale,
+                long long max_steps, bool with_hist, cudaStream_t s) {
+  if (p->cfg.dtype == AMX_F32) {
+    auto a = make_fv_args<float>(p, state, prm, mode);
+    a.dt_in = dt_in;
+    a.dt_scale = dt_scale;
+    a.max_steps = max_steps;
+    return fv_launch(p, a, s);
+  }
+  auto a = make_fv_args<double>(p, state, prm, mode);
+  a.dt_in = dt_in;
+  a.dt_scale = dt_scale;
+  a.max_steps = max_steps;
+  (void)with_hist;
+  return fv_launch(p, a, s);
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+
+extern "C" {
+
+const char* amx_version(void) { return "amx 0.1.0 (sm_103a)"; }
+
+int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out) {
+  if (!out) return AMX_ERR_INVALID_ARG;
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  if (max_history < 0) return AMX_ERR_INVALID_ARG;
+  amx_plan* p = new (std::nothrow) amx_plan();
+  if (!p) return AMX_ERR_INVALID_ARG;
+  p->cfg = *cfg;
+  p->elem = cfg->dtype == AMX_F32 ? 4 : 8;
+  p->ncells = ipow(cfg->num_cells, cfg->dimensionality);
+  if (cudaGetDevice(&p->device) != cudaSuccess) { delete p; return AMX_ERR_CUDA; }
+  cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->device);
+  if (cudaMalloc(&p->diag, 8 * sizeof(double)) != cudaSuccess) { delete p; return AMX_ERR_CUDA; }
+
+  if (cfg->solver_mode == AMX_FINITE_DIFFERENCE) {
+    rc = amx::fd_plan_create(*cfg, max_history, &p->fd);
+    if (rc) { cudaFree(p->diag); delete p; return rc; }
+    *out = p;
+    return AMX_OK;
+  }
+
+  // ---- FV kernel selection
+  const int rs = (cfg->riemann_solver == AMX_HLLC_LM) ? AMX_HLLC : cfg->riemann_solver;
+  const bool ok = (cfg->dtype == AMX_F32) ? amx::fv_kernel_f32(cfg->dimensionality, rs, cfg->mhd != 0, &p->fv)
+                                          : amx::fv_kernel_f64(cfg->dimensionality, rs, cfg->mhd != 0, &p->fv);
+  if (!ok) { amx_plan_destroy(p); return AMX_ERR_UNSUPPORTED; }
+  if (cudaFuncSetAttribute(p->fv.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fv.smem) != cudaSuccess) {
+    amx_plan_destroy(p);
+    return AMX_ERR_CUDA;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, p->fv.fn, amx::kFVThreads, p->fv.smem) != cudaSuccess ||
+      per_sm < 1) {
+    amx_plan_destroy(p);
+    return AMX_ERR_CUDA;
+  }
+  const long long cap = (long long)per_sm * p->num_sms;
+  const long long need = std::max<long long>(1, (p->ncells + amx::kFVThreads - 1) / amx::kFVThreads);
+  p->fv_grid = (int)std::min<long long>(cap, need);
+
+  // ---- workspace: stage buffer, two magnetic iterate buffers, control, history
+  const int nv_gas = cfg->dimensionality + 2;
+  const size_t field = (size_t)p->ncells * p->elem;
+  size_t off = 0;
+  const size_t o_p1 = off; off = align256(off + nv_gas * field);
+  const size_t o_m0 = off; off = align256(off + (cfg->mhd ? 6 : 0) * field);
+  const size_t o_m1 = off; off = align256(off + (cfg->mhd ? 6 : 0) * field);
+  const size_t o_ctl = off; off = align256(off + sizeof(FVControl));
+  const size_t o_dth = off; off = align256(off + sizeof(double) * (size_t)max_history);
+  const size_t o_ith = off; off = align256(off + sizeof(int) * (size_t)max_history);
+  p->ws_bytes = off;
+  if (cudaMalloc(&p->ws, p->ws_bytes) != cudaSuccess) { amx_plan_destroy(p); return AMX_ERR_CUDA; }
+  cudaMemset(p->ws, 0, p->ws_bytes);
+  p->p1 = p->ws + o_p1;
+  p->mag0 = p->ws + o_m0;
+  p->mag1 = p->ws + o_m1;
+  p->ctl = reinterpret_cast<FVControl*>(p->ws + o_ctl);
+  p->max_hist = max_history;
+  p->dt_hist = max_history ? reinterpret_cast<double*>(p->ws + o_dth) : nullptr;
+  p->it_hist = max_history ? reinterpret_cast<int*>(p->ws + o_ith) : nullptr;
+  if (cudaDeviceSynchronize() != cudaSuccess) { amx_plan_destroy(p); return AMX_ERR_CUDA; }
+  *out = p;
+  return AMX_OK;
+}
+
+int amx_plan_destroy(amx_plan* p) {
+  if (!p) return AMX_OK;
+  if (p->diag) cudaFree(p->diag);
+  if (p->fd) amx::fd_plan_destroy(p->fd);
+  if (p->ws) cudaFree(p->ws);
+  delete p;
+  return AMX_OK;
+}
+
+int amx_plan_workspace_bytes(const amx_plan* p, size_t* bytes) {
+  if (!p || !bytes) return AMX_ERR_INVALID_ARG;
+  *bytes = p->fd ? amx::fd_workspace_bytes(p->fd) : p->ws_bytes;
+  return AMX_OK;
+}
+
+int amx_plan_reset(amx_plan* p, void* stream) {
+  if (!p) return AMX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->fd) return amx::fd_reset(p->fd, s);
+  return cuda_ok(cudaMemsetAsync(p->ctl, 0, sizeof(FVControl), s));
+}
+
+int amx_plan_set_time(amx_plan* p, double t, void* stream) {
+  if (!p) return AMX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->fd) return amx::fd_set_time(p->fd, t, s);
+  return cuda_ok(cudaMemcpyAsync(&p->ctl->t, &t, sizeof(double), cudaMemcpyHostToDevice, s)) |
+         cuda_ok(cudaStreamSynchronize(s));
+}
+
+int amx_cfl_dt(amx_plan* p, const void* state, const amx_params* prm, double* dt_host, void* stream) {
+  if (!p || !state || !prm || !dt_host) return AMX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->fd) return amx::fd_cfl_dt(p->fd, state, *prm, dt_host, s);
+  int rc = fv_run_mode(p, const_cast<void*>(state), prm, amx::FV_MODE_CFL, 0.0, 1.0, 0, false, s);
+  if (rc) return rc;
+  rc = cuda_ok(cudaMemcpyAsync(dt_host, &p->ctl->dt, sizeof(double), cudaMemcpyDeviceToHost, s));
+  rc |= cuda_ok(cudaStreamSynchronize(s));
+  return rc;
+}
+
+int amx_fv_hydro_rk2(amx_plan* p, void* state, const amx_params* prm, double dt, void* stream) {
+  if (!p || !state || !prm || p->fd) return AMX_ERR_INVALID_ARG;
+  return fv_run_mode(p, state, prm, amx::FV_MODE_HYDRO_RK2, dt, 1.0, 0, false, static_cast<cudaStream_t>(stream));
+}
+
+int amx_fv_magnetic_update(amx_plan* p, void* state, const amx_params* prm, double dt, void* stream) {
+  if (!p || !state || !prm || p->fd) return AMX_ERR_INVALID_ARG;
+  if (!p->cfg.mhd) return AMX_ERR_INVALID_ARG;
+  return fv_run_mode(p, state, prm, amx::FV_MODE_MAGNETIC, dt, 1.0, 0, false, static_cast<cudaStream_t>(stream));
+}
+
+int amx_evolve_state(amx_plan* p, void* state, const amx_params* prm, double dt, void* stream) {
+  if (!p || !state || !prm) return AMX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->fd) return amx::fd_evolve(p->fd, state, *prm, dt, s);
+  return fv_run_mode(p, state, prm, amx::FV_MODE_EVOLVE, dt, 1.0, 0, false, s);
+}
+
+static int fv_run_steps(amx_plan* p, void* state, const amx_params* prm, int64_t max_steps, cudaStream_t s) {
+  // one cooperative launch per chunk; the kernel stops by itself at t_end
+  const int64_t chunk = 1 << 16;
+  int64_t done = 0;
+  while (done < max_steps) {
+    const int64_t k = std::min<int64_t>(chunk, max_steps - done);
+    int rc;
+    if (p->cfg.dtype == AMX_F32) {
+      auto a = make_fv_args<float>(p, state, prm, amx::FV_MODE_STEPS);
+      a.max_steps = k;
+      rc = fv_launch(p, a, s);
+    } else {
+      auto a = make_fv_args<double>(p, state, prm, amx::FV_MODE_STEPS);
+      a.max_steps = k;
+      rc = fv_launch(p, a, s);
+    }
+    if (rc) return rc;
+    done += k;
+  }
+  return AMX_OK;
+}
+
+int amx_run_async(amx_plan* p, void* state, const amx_params* prm, int64_t max_steps, void* stream) {
+  if (!p || !state || !prm || max_steps < 0) return AMX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->fd) return amx::fd_run(p->fd, state, *prm, max_steps, INFINITY, s);
+  return fv_run_steps(p, state, prm, max_steps, s);
+}
+
+static int read_info(amx_plan* p, amx_run_info* info, cudaStream_t s) {
+  if (p->fd) return amx::fd_info(p->fd, info, s);
+  FVControl h;
+  int rc = cuda_ok(cudaMemcpyAsync(&h, p->ctl, sizeof(FVControl), cudaMemcpyDeviceToHost, s));
+  rc |= cuda_ok(cudaStreamSynchronize(s));
+  if (rc) return rc;
+  info->t = h.t;
+  info->last_dt = h.dt;
+  info->steps = h.steps;
+  info->magnetic_iterations = h.mag_iters_total;
+  info->last_magnetic_iterations = h.mag_iters;
+  info->status = h.status;
+  return AMX_OK;
+}
+
+int amx_run(amx_plan* p, void* state, const amx_params* prm, int64_t max_steps, amx_run_info* info, void* stream) {
+  return amx_run_until(p, state, prm, max_steps, INFINITY, info, stream);
+}
+
+int amx_run_until(amx_plan* p, void* state, const amx_params* prm, int64_t max_steps, double t_pause,
+                  amx_run_info* info, void* stream) {
+  if (!p || !state || !prm || max_steps < 0) return AMX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->fd) {
+    int rc = amx::fd_run(p->fd, state, *prm, max_steps, t_pause, s);
+    if (rc) return rc;
+    amx_run_info tmp;
+    return read_info(p, info ? info : &tmp, s);
+  }
+  // FV: the history records are indexed from the first step of this call
+  int rc = AMX_OK;
+  const int64_t chunk = 1 << 16;
+  int64_t done = 0;
+  amx_run_info tmp{};
+  while (done < max_steps) {
+    const int64_t k = std::min<int64_t>(chunk, max_steps - done);
+    if (p->cfg.dtype == AMX_F32) {
+      auto a = make_fv_args<float>(p, state, prm, amx::FV_MODE_STEPS);
+      a.max_steps = k;
+      a.t_pause = t_pause;
+      rc = fv_launch(p, a, s);
+    } else {
+      auto a = make_fv_args<double>(p, state, prm, amx::FV_MODE_STEPS);
+      a.max_steps = k;
+      a.t_pause = t_pause;
+      rc = fv_launch(p, a, s);
+    }
+    if (rc) return rc;
+    rc = read_info(p, &tmp, s);
+    if (rc) return rc;
+    done += k;
+    if (!p->cfg.fixed_timestep && !(tmp.t < prm->t_end)) break;
+    if (tmp.t >= t_pause) break;
+    if (tmp.status & (AMX_ERR_TIMEOUT | AMX_ERR_NAN)) break;
+  }
+  if (info) *info = tmp;
+  return AMX_OK;
+}
+
+int amx_history(amx_plan* p, double* dt_host, int32_t* iters_host, int64_t n, void* stream) {
+  if (!p || n < 0) return AMX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->fd) return amx::fd_history(p->fd, dt_host, n, s);
+  if (n > p->max_hist) return AMX_ERR_INVALID_ARG;
+  int rc = AMX_OK;
+  if (dt_host && n) rc |= cuda_ok(cudaMemcpyAsync(dt_host, p->dt_hist, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+  if (iters_host && n) rc |= cuda_ok(cudaMemcpyAsync(iters_host, p->it_hist, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  rc |= cuda_ok(cudaStreamSynchronize(s));
+  return rc;
+}
+
+int amx_conservation_sums(amx_plan* p, const void* state, const amx_params* prm, double out_host[5],
+                          void* stream) {
+  if (!p || !state || !prm || !out_host) return AMX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  amx_config c = p->cfg;
+  if (c.solver_mode == AMX_FINITE_DIFFERENCE) c.dimensionality = 3;
+  int rc = amx_diag_sums_raw(&c, state, prm->gamma, p->diag, stream);
+  if (rc) return rc;
+  double h[5];
+  rc = cuda_ok(cudaMemcpyAsync(h, p->diag, sizeof(h), cudaMemcpyDeviceToHost, s));
+  rc |= cuda_ok(cudaStreamSynchronize(s));
+  if (rc) return rc;
+  const int d = c.dimensionality;
+  const double dv = std::pow(c.grid_spacing, d);
+  // total_quantities.py:155-176: 1D sums rho * cell volume (dx), 2D/3D sum(rho) * box^d
+  out_host[0] = (d == 1) ? h[0] * c.grid_spacing : h[0] * std::pow(c.box_size, d);
+  out_host[1] = h[1] * dv;
+  out_host[2] = h[2] * dv;
+  out_host[3] = h[3] * dv;
+  out_host[4] = h[4];
+  return AMX_OK;
+}
+
+int amx_status(amx_plan* p, int32_t* status_host, int32_t clear, void* stream) {
+  if (!p || !status_host) return AMX_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->fd) return amx::fd_status(p->fd, status_host, clear, s);
+  int rc = cuda_ok(cudaMemcpyAsync(status_host, &p->ctl->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  rc |= cuda_ok(cudaStreamSynchronize(s));
+  if (clear) rc |= cuda_ok(cudaMemsetAsync(&p->ctl->status, 0, sizeof(int), s));
+  rc |= cuda_ok(cudaStreamSynchronize(s));
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,249 @@
+"""The drop-in time driver: ``time_integration(state, config, params, rv)``.
+
+Same signature and return types as astronomix's time_integration
+(astronomix/time_stepping/time_integration.py:61-236).  The state may be a
+NumPy array or a torch tensor (CPU or CUDA), float32 or float64; the result
+comes back in the same form.  The whole loop runs on the GPU through the C
+ABI (include/amx.h): the host only launches and, when snapshots are
+requested, pauses at the snapshot times.
+"""
+
+from typing import NamedTuple, Any
+import math
+
+import numpy as np
+
+from . import _native
+from .option_classes import (
+    FINITE_VOLUME, FINITE_DIFFERENCE, GHOST_CELLS, PERIODIC_ROLL, PERIODIC_BOUNDARY, OPEN_BOUNDARY,
+    UNSPLIT, RK2_SSP, CARTESIAN, SimulationConfig, SimulationParams, BoundarySettings1D,
+)
+from .variable_registry import RegisteredVariables
+
+
+class SnapshotData(NamedTuple):
+    """Return format when snapshots are requested (data_classes/simulation_snapshot_data.py:5-45)."""
+
+    time_points: Any = None
+    states: Any = None
+    final_state: Any = None
+    total_mass: Any = None
+    total_energy: Any = None
+    internal_energy: Any = None
+    kinetic_energy: Any = None
+    gravitational_energy: Any = None
+    radial_momentum: Any = None
+    magnetic_divergence: Any = None
+    runtime: float = 0.0
+    num_iterations: int = 0
+    current_checkpoint: int = 0
+
+
+class StateStruct(NamedTuple):
+    primitive_state: Any = None
+
+
+def _check_supported(config: SimulationConfig):
+    if config.geometry != CARTESIAN:
+        raise NotImplementedError("only Cartesian geometry is part of the accelerated path")
+    if config.self_gravity:
+        raise NotImplementedError("self-gravity is not part of the accelerated MHD step")
+    if config.wind_config.stellar_wind or config.cooling_config.cooling or \
+            config.cosmic_ray_config.cosmic_rays or config.neural_net_force_config.neural_net_force or \
+            config.cnn_mhd_corrector_config.cnn_mhd_corrector or \
+            config.turbulent_forcing_config.turbulent_forcing:
+        raise NotImplementedError("physics modules are not part of the accelerated MHD step")
+    if config.solver_mode == FINITE_VOLUME:
+        if config.split != UNSPLIT:
+            raise NotImplementedError("the split (MUSCL-Hancock) FV scheme is not part of the accelerated path")
+        if config.time_integrator != RK2_SSP:
+            raise ValueError("Only the RK2 SSP time integrator is currently supported for the unsplit scheme.")
+    if config.use_specific_snapshot_timepoints:
+        raise NotImplementedError("specific snapshot time points are not supported yet")
+
+
+def _bc_codes(config: SimulationConfig):
+    lo, hi = [PERIODIC_BOUNDARY] * 3, [PERIODIC_BOUNDARY] * 3
+    bs = config.boundary_settings
+    if bs is None:
+        bs = BoundarySettings1D(OPEN_BOUNDARY, OPEN_BOUNDARY) if config.dimensionality == 1 else None
+    if isinstance(bs, BoundarySettings1D):
+        lo[0], hi[0] = bs.left_boundary, bs.right_boundary
+    elif bs is not None:
+        for k, b in enumerate((bs.x, bs.y, bs.z)):
+            lo[k], hi[k] = b.left_boundary, b.right_boundary
+    else:
+        lo, hi = [OPEN_BOUNDARY] * 3, [OPEN_BOUNDARY] * 3
+    return lo, hi
+
+
+def make_amx_config(config: SimulationConfig, rv: RegisteredVariables, shape, dtype) -> _native.amx_config:
+    """Translate a (finalised) SimulationConfig into the C struct."""
+    c = _native.amx_config()
+    c.solver_mode = int(config.solver_mode)
+    c.dtype = _native.AMX_F64 if np.dtype(dtype) == np.float64 else _native.AMX_F32
+    c.dimensionality = int(config.dimensionality)
+    c.num_cells = int(shape[-1])
+    c.num_vars = int(shape[0])
+    c.mhd = int(bool(config.mhd))
+    c.riemann_solver = int(config.riemann_solver)
+    c.limiter = int(config.limiter)
+    c.fv_magnetic_integrator = int(config.fv_magnetic_integrator)
+    c.numerical_precision = int(config.numerical_precision)
+    c.boundary_handling = int(config.boundary_handling)
+    lo, hi = _bc_codes(config)
+    for k in range(3):
+        c.bc_lo[k] = int(lo[k])
+        c.bc_hi[k] = int(hi[k])
+    c.enforce_positivity = int(bool(config.enforce_positivity))
+    c.exact_end_time = int(bool(config.exact_end_time))
+    c.fixed_timestep = int(bool(config.fixed_timestep))
+    c.num_timesteps = int(config.num_timesteps)
+    c.box_size = float(config.box_size)
+    c.grid_spacing = float(config.grid_spacing)
+    return c
+
+
+_PLANS = {}
+
+
+def get_plan(config, rv, shape, dtype, max_history=0):
+    key = (config, rv, tuple(shape), np.dtype(dtype).str, int(max_history))
+    plan = _PLANS.get(key)
+    if plan is None:
+        plan = _native.Plan(make_amx_config(config, rv, shape, dtype), max_history)
+        _PLANS[key] = plan
+    return plan
+
+
+def _to_device(state):
+    """-> (cuda tensor, restore function)."""
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("astronomix_gb300 runs on a CUDA GPU; no device is visible")
+    if isinstance(state, torch.Tensor):
+        was_cuda = state.is_cuda
+        dev = state.detach().to("cuda").contiguous().clone()
+
+        def restore(t):
+            return t if was_cuda else t.cpu()
+
+        return dev, restore
+    arr = np.ascontiguousarray(state)
+    if arr.dtype not in (np.float32, np.float64):
+        arr = arr.astype(np.float32)
+    dev = torch.from_numpy(arr).to("cuda")
+
+    def restore(t):
+        return t.cpu().numpy()
+
+    return dev, restore
+
+
+def _stream():
+    import torch
+
+    return torch.cuda.current_stream().cuda_stream
+
+
+def time_integration(primitive_state, config: SimulationConfig, params: SimulationParams,
+                     registered_variables: RegisteredVariables, snapshot_callable=None, sharding=None):
+    """Integrate to ``params.t_end`` on the GPU (time_integration.py:61-236).
+
+    ``sharding`` is accepted for signature compatibility and ignored: one
+    simulation runs on one GPU.
+    """
+    _check_supported(config)
+    if config.state_struct:
+        primitive_state = primitive_state.primitive_state
+    import torch
+
+    dev, restore = _to_device(primitive_state)
+    shape = tuple(dev.shape)
+    np_dtype = np.float64 if dev.dtype == torch.float64 else np.float32
+    if dev.dtype not in (torch.float32, torch.float64):
+        dev = dev.float()
+    plan = get_plan(config, registered_variables, shape, np_dtype)
+    prm = _native.make_params(params)
+    stream = _stream()
+    plan.reset(stream)
+    ptr = dev.data_ptr()
+    huge = 1 << 62
+    max_steps = int(config.num_timesteps) if config.fixed_timestep else huge
+
+    if not (config.return_snapshots or config.activate_snapshot_callback):
+        info = plan.run(ptr, prm, max_steps, stream)
+        _raise_status(info.status, config)
+        out = restore(dev)
+        return StateStruct(primitive_state=out) if config.state_struct else out
+
+    # ---- snapshots: pause before the first step starting at t >= k t_end / n
+    n = int(config.num_snapshots)
+    ss = config.snapshot_settings
+    times, states, mass, energy, internal, kinetic, divb = [], [], [], [], [], [], []
+    k = 0
+    steps_taken = 0
+    while True:
+        thr = k * params.t_end / n if k < n else math.inf
+        info = plan.run_until(ptr, prm, max_steps - steps_taken, thr, stream)
+        _raise_status(info.status, config)
+        steps_taken = info.steps
+        done = (steps_taken >= max_steps) or (not config.fixed_timestep and not (info.t < params.t_end))
+        if done:
+            break
+        # at the start of a step with t >= threshold k
+        if config.return_snapshots:
+            times.append(info.t)
+            if ss.return_states:
+                states.append(restore(dev.clone()))
+            sums = plan.conservation_sums(ptr, prm, stream)
+            mass.append(sums[0])
+            energy.append(sums[1])
+            kinetic.append(sums[2])
+            internal.append(sums[3])
+            divb.append(sums[4])
+        if config.activate_snapshot_callback and snapshot_callable is not None:
+            snapshot_callable(info.t, restore(dev.clone()), registered_variables)
+        k += 1
+        info = plan.run(ptr, prm, 1, stream)
+        _raise_status(info.status, config)
+        steps_taken = info.steps
+        if steps_taken >= max_steps or (not config.fixed_timestep and not (info.t < params.t_end)):
+            break
+
+    final = restore(dev)
+    if not config.return_snapshots:
+        return StateStruct(primitive_state=final) if config.state_struct else final
+
+    def pad(lst):
+        a = np.zeros(n)
+        a[:len(lst)] = lst[:n]
+        return a
+
+    st = None
+    if ss.return_states:
+        st = np.zeros((n, *shape), dtype=np_dtype)
+        for i, s in enumerate(states[:n]):
+            st[i] = np.asarray(s.cpu() if hasattr(s, "cpu") else s)
+    return SnapshotData(
+        time_points=pad(times),
+        states=st,
+        final_state=final if ss.return_final_state else None,
+        total_mass=pad(mass) if ss.return_total_mass else None,
+        total_energy=pad(energy) if ss.return_total_energy else None,
+        internal_energy=pad(internal) if ss.return_internal_energy else None,
+        kinetic_energy=pad(kinetic) if ss.return_kinetic_energy else None,
+        magnetic_divergence=pad(divb) if (ss.return_magnetic_divergence and config.mhd) else None,
+        num_iterations=int(steps_taken),
+        current_checkpoint=min(k, n),
+    )
+
+
+def _raise_status(status, config):
+    hard = status & (_native.AMX_ERR_TIMEOUT | _native.AMX_ERR_BOUNDS | _native.AMX_ERR_CUDA)
+    if hard:
+        raise _native.AmxError(status, "time_integration")
+    if config.runtime_debugging and status & (_native.AMX_ERR_NAN | _native.AMX_ERR_NEGATIVE |
+                                              _native.AMX_ERR_NOT_CONVERGED):
+        raise FloatingPointError(str(_native.AmxError(status, "time_integration")))

@@ -1,0 +1,202 @@
+/*
+ * amx -- GB300-native MHD step of astronomix, C ABI.
+ *
+ * Plain C: integers, doubles, opaque handles and raw device pointers.  No
+ * torch, JAX or C++ types cross this boundary and nothing here throws.
+ *
+ * Every entry point returns 0 on success or a bitwise OR of AMX_ERR_* codes.
+ * Device-side numerical conditions (NaN, fixed-point cap, barrier timeout)
+ * are accumulated in the plan's status word and read with amx_status().
+ * Entry points are stream-ordered on the caller's stream (a cudaStream_t
+ * passed as void*); none of them synchronises the stream unless its comment
+ * says so.
+ *
+ * State arrays are the reference's layout: state[var][x][y][z], C order,
+ * without ghost cells, in float32 or float64 (amx_config.dtype), with the
+ * row order of astronomix/variable_registry/registered_variables.py:116-238.
+ */
+#ifndef AMX_H_
+#define AMX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status / error bits ------------------------------------------------ */
+#define AMX_OK 0
+#define AMX_ERR_INVALID_ARG (1 << 0)   /* bad pointer, size or option      */
+#define AMX_ERR_CUDA (1 << 1)          /* a CUDA runtime call failed       */
+#define AMX_ERR_NAN (1 << 2)           /* non-finite value met on device   */
+#define AMX_ERR_NEGATIVE (1 << 3)      /* negative density or pressure     */
+#define AMX_ERR_NOT_CONVERGED (1 << 4) /* magnetic fixed point hit its cap */
+#define AMX_ERR_TIMEOUT (1 << 5)       /* bounded grid barrier gave up     */
+#define AMX_ERR_BOUNDS (1 << 6)        /* index check failed               */
+#define AMX_ERR_UNSUPPORTED (1 << 7)   /* option outside the kernels       */
+#define AMX_ERR_TOO_LARGE (1 << 8)     /* size above a fixed limit         */
+
+/* ---- enumerations (values equal the reference's constants,
+ *      astronomix/option_classes/simulation_config.py:20-93) --------------- */
+#define AMX_F32 0
+#define AMX_F64 1
+
+#define AMX_FINITE_VOLUME 0
+#define AMX_FINITE_DIFFERENCE 1
+
+#define AMX_HLL 0
+#define AMX_HLLC 1
+#define AMX_HLLC_LM 2
+#define AMX_LAX_FRIEDRICHS 3
+
+#define AMX_MINMOD 0
+#define AMX_OSHER 1
+#define AMX_DOUBLE_MINMOD 2
+#define AMX_SUPERBEE 3
+#define AMX_VAN_ALBADA 4
+
+#define AMX_BC_OPEN 0
+#define AMX_BC_REFLECTIVE 1
+#define AMX_BC_PERIODIC 2
+
+#define AMX_GHOST_CELLS 0
+#define AMX_PERIODIC_ROLL 1
+
+#define AMX_IMPLICIT_MIDPOINT 0
+#define AMX_IMPLICIT_EULER 1
+
+/* Static configuration: the fields of SimulationConfig that select kernels
+ * (astronomix/option_classes/simulation_config.py:160-342). */
+typedef struct amx_config {
+  int32_t solver_mode;            /* AMX_FINITE_VOLUME / AMX_FINITE_DIFFERENCE  */
+  int32_t dtype;                  /* AMX_F32 / AMX_F64 (storage and arithmetic) */
+  int32_t dimensionality;         /* 1, 2 or 3                                  */
+  int32_t num_cells;              /* cells per axis (square / cubic grids)      */
+  int32_t num_vars;               /* rows of the state array                    */
+  int32_t mhd;                    /* 0 / 1                                      */
+  int32_t riemann_solver;         /* AMX_HLL .. AMX_LAX_FRIEDRICHS              */
+  int32_t limiter;                /* AMX_MINMOD .. AMX_VAN_ALBADA               */
+  int32_t fv_magnetic_integrator; /* AMX_IMPLICIT_MIDPOINT / _EULER             */
+  int32_t numerical_precision;    /* 0: fixed-point tol 1e-5, 1: 1e-10          */
+  int32_t boundary_handling;      /* AMX_GHOST_CELLS / AMX_PERIODIC_ROLL        */
+  int32_t bc_lo[3];               /* per axis AMX_BC_*                          */
+  int32_t bc_hi[3];
+  int32_t enforce_positivity;     /* FD floors                                  */
+  int32_t exact_end_time;
+  int32_t fixed_timestep;
+  int32_t num_timesteps;
+  double box_size;
+  double grid_spacing;            /* box_size / num_cells                       */
+} amx_config;
+
+/* Traced parameters (astronomix/option_classes/simulation_params.py:11-66). */
+typedef struct amx_params {
+  double C_cfl;
+  double gamma;
+  double minimum_density;
+  double minimum_pressure;
+  double dt_max;
+  double t_end;
+} amx_params;
+
+/* Result of a time-integration call. */
+typedef struct amx_run_info {
+  double t;                       /* simulation time reached              */
+  double last_dt;                 /* dt of the last step                  */
+  int64_t steps;                  /* total steps taken by this plan       */
+  int64_t magnetic_iterations;    /* total FV fixed-point iterations      */
+  int32_t last_magnetic_iterations;
+  int32_t status;                 /* AMX_ERR_* bits seen on the device    */
+} amx_run_info;
+
+typedef struct amx_plan amx_plan;
+
+/* ---- plan lifecycle ----------------------------------------------------- */
+
+/* Validates `cfg` (the checks of finalize_config,
+ * astronomix/option_classes/simulation_config.py:345-470, that concern the
+ * kernels) and allocates the plan's device workspace on the current device.
+ * `max_history` (>= 0) sizes the per-step dt / iteration record. */
+int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out);
+int amx_plan_destroy(amx_plan* plan);
+/* Bytes of device workspace the plan holds. */
+int amx_plan_workspace_bytes(const amx_plan* plan, size_t* bytes);
+/* Resets time, step counters, history and status to zero (stream-ordered). */
+int amx_plan_reset(amx_plan* plan, void* stream);
+/* Sets the time accumulator (used by drivers that restart a run). */
+int amx_plan_set_time(amx_plan* plan, double t, void* stream);
+
+/* ---- step-level seams ---------------------------------------------------- */
+
+/* Replaces _cfl_time_step, astronomix/_finite_volume/_timestep_estimation/
+ * _timestep_estimator.py:95-218 (UNSPLIT branch), and _cfl_time_step_fd,
+ * astronomix/_finite_difference/_timestep_estimation/_timestep_estimator.py:26-91.
+ * Writes the FP64 dt to *dt_host (synchronises the stream). */
+int amx_cfl_dt(amx_plan* plan, const void* state, const amx_params* prm, double* dt_host,
+               void* stream);
+
+/* Replaces _evolve_gas_state_unsplit (one SSP-RK2 update of the gas rows),
+ * astronomix/_finite_volume/_state_evolution/evolve_state.py:419-488, with
+ * time step dt.  `state` holds the full state; only gas rows change. */
+int amx_fv_hydro_rk2(amx_plan* plan, void* state, const amx_params* prm, double dt, void* stream);
+
+/* Replaces magnetic_update,
+ * astronomix/_finite_volume/_magnetic_update/_magnetic_field_update.py:37-242.
+ * Updates B rows, gas velocity and pressure in place. */
+int amx_fv_magnetic_update(amx_plan* plan, void* state, const amx_params* prm, double dt,
+                           void* stream);
+
+/* Replaces _evolve_state_fv,
+ * astronomix/_finite_volume/_state_evolution/evolve_state.py:497-600, and
+ * _evolve_state_fd, astronomix/_finite_difference/_state_evolution/
+ * _evolve_state.py:25-73: one step of size dt, in place. */
+int amx_evolve_state(amx_plan* plan, void* state, const amx_params* prm, double dt, void* stream);
+
+/* ---- time driver --------------------------------------------------------- */
+
+/* Replaces the loop of _time_integration,
+ * astronomix/time_stepping/time_integration.py:386-801 (adaptive dt with
+ * exact end time, or the fixed-step loop): advances `state` in place until
+ * t >= prm->t_end or `max_steps` more steps were taken, without a host round
+ * trip per step.  Synchronises the stream and fills *info when non-null. */
+int amx_run(amx_plan* plan, void* state, const amx_params* prm, int64_t max_steps,
+            amx_run_info* info, void* stream);
+
+/* amx_run that also stops before the first step starting at t >= t_pause
+ * (the snapshot points of time_integration.py:556-566). */
+int amx_run_until(amx_plan* plan, void* state, const amx_params* prm, int64_t max_steps, double t_pause,
+                  amx_run_info* info, void* stream);
+
+/* Like amx_run but does not synchronise: launches exactly the work of
+ * `max_steps` steps (steps after t_end are skipped on the device).  For
+ * timing and for callers that overlap host work. */
+int amx_run_async(amx_plan* plan, void* state, const amx_params* prm, int64_t max_steps,
+                  void* stream);
+
+/* Copies the per-step dt record (FP64) and fixed-point iteration counts of
+ * the steps taken since the last reset into host arrays of length `n`
+ * (synchronises).  Either pointer may be null. */
+int amx_history(amx_plan* plan, double* dt_host, int32_t* iters_host, int64_t n, void* stream);
+
+/* ---- diagnostics ---------------------------------------------------------- */
+
+/* FP64 global sums of the state (astronomix/_fluid_equations/total_quantities.py:
+ * 31-176): out[0] = total mass, out[1] = total energy, out[2] = kinetic
+ * energy, out[3] = internal energy, out[4] = max |div B| (0 without MHD).
+ * Synchronises the stream. */
+int amx_conservation_sums(amx_plan* plan, const void* state, const amx_params* prm,
+                          double out_host[5], void* stream);
+
+/* Reads (and with clear != 0 resets) the plan's device status bits.
+ * Synchronises the stream. */
+int amx_status(amx_plan* plan, int32_t* status_host, int32_t clear, void* stream);
+
+/* Library version string. */
+const char* amx_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AMX_H_ */
