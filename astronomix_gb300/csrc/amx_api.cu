@@ -379,6 +379,10 @@ int amx_run_until(amx_plan* p, void* state, const amx_params* prm, int64_t max_s
     if (tmp.t >= t_pause) break;
     if (tmp.status & (AMX_ERR_TIMEOUT | AMX_ERR_NAN)) break;
   }
+  if (max_steps == 0) {
+    rc = read_info(p, &tmp, s);
+    if (rc) return rc;
+  }
   if (info) *info = tmp;
   return AMX_OK;
 }

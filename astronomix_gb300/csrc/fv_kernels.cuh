@@ -280,7 +280,7 @@ __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __re
           qR[v] = q0 - g0 * dxT / T(2);
         }
         T F[NV];
-        riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), F);
+        riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), a.lm != 0, F);
         // face f stored at its own (E0,E1,E2) index
 #pragma unroll
         for (int v = 0; v < NV; ++v) sF[v * G::FMAX + f] = F[v];

@@ -243,10 +243,11 @@ __device__ __forceinline__ void lf_flux(const T* qL, const T* qR, int d, T gamma
   for (int v = 0; v < NV; ++v) F[v] = T(0.5) * (FL[v] + FR[v]) - ha * (UR[v] - UL[v]);
 }
 
+// `lm` selects the HLLC-LM variant inside the HLLC family (runtime flag)
 template <typename T, int DIM, int RS>
-__device__ __forceinline__ void riemann(const T* qL, const T* qR, int d, T gamma, T alpha, T* F) {
+__device__ __forceinline__ void riemann(const T* qL, const T* qR, int d, T gamma, T alpha, bool lm, T* F) {
   if (RS == RS_HLL) hll_flux<T, DIM>(qL, qR, d, gamma, F);
-  else if (RS == RS_HLLC) hllc_flux<T, DIM>(qL, qR, d, gamma, false, F);
+  else if (RS == RS_HLLC) hllc_flux<T, DIM>(qL, qR, d, gamma, lm, F);
   else if (RS == RS_HLLC_LM) hllc_flux<T, DIM>(qL, qR, d, gamma, true, F);
   else lf_flux<T, DIM>(qL, qR, d, gamma, alpha, F);
 }

@@ -1,0 +1,386 @@
+"""Benchmark: zone-updates/s of the FV MHD step on the 2D Orszag-Tang vortex, 512^2, FP32.
+
+One "step" is one time step of astronomix's finite-volume MHD scheme (CFL dt,
+SSP-RK2 hydro half step, implicit-midpoint magnetic sub-step, hydro half step)
+over the whole 512^2 grid, launched through the C ABI.  The Orszag-Tang state
+is synthetic (its analytic initial condition, advanced by warm-up steps).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Timing: each timed step is bracketed by CUDA events on the launching stream
+and the L2 cache (129 MB; the state is 7.3 MB) is flushed between steps by
+writing a 512 MB buffer, outside the events.  The line also carries the
+end-to-end number through the C ABI with host buffers (H2D + step + D2H per
+step), the FP64 throughput of the same kernels, the FP32-vs-FP64 L1 density
+error at t = 0.05, the roofline of the kernel and the CPU baseline (the
+oracle, a NumPy restatement of the reference, timed on this host).
+
+With N > 1 (torchrun), every rank runs an independent replica of the
+workload (the step does not shard); value = sum of zone-updates / max time.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+N_CELLS = 512
+METRIC = "zone-updates/s on 1 GB300, FP32 fused vs plain FP64, at L1 err <=1e-5 vs FP64"
+WORKLOAD = "Orszag-Tang 2D MHD, FV HLL + Pang-Wu split (constrained B), MINMOD, SSP-RK2, 512x512 periodic, gamma 5/3"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_CELLS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    rank, world = 0, 1
+    if args.gpus > 1 or "WORLD_SIZE" in os.environ:
+        import torch
+        import torch.distributed as dist
+
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        if world > 1:
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.samples = []
+        self.proc = None
+        self.device_index = device_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def algorithmic_bytes_per_zone_update(k_mean, elem=4):
+    # FV 2D MHD: hydro RK2 half steps 2 x 20 words + magnetic 16 words per
+    # fixed-point evaluation x (k + 1) + 6 words of write-back
+    return elem * (46 + 16 * (k_mean + 1))
+
+
+def load_traffic(name):
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(name)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline_oracle(budget_s=15.0, n=128):
+    """The oracle (NumPy restatement of the reference) on a bounded sample: OT n^2, FP32."""
+    from _cases import orszag_tang
+    from oracle import driver
+
+    cfg, prm, rv, s = orszag_tang(n=n, t_end=10.0, dtype=np.float32)
+    P = s
+    steps = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s:
+        P = driver.time_integration(P, cfg, prm, rv, max_steps=1)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return {"value": n * n * steps / dt, "unit": "zone-updates/s", "cores": 1, "kind": "port",
+            "sample": "oracle (NumPy restatement) OT %dx%d FP32, %d steps in %.1f s" % (n, n, steps, dt)}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the oracle port of the reference's CPU path on this host."""
+    if rank != 0:
+        return
+    from _cases import orszag_tang
+    from oracle import driver
+
+    cfg, prm, rv, s = orszag_tang(n=args.n, t_end=10.0, dtype=np.float32)
+    P = s
+    for _ in range(max(1, min(args.warmup, 1))):
+        P = driver.time_integration(P, cfg, prm, rv, max_steps=1)
+    times = []
+    budget = 60.0
+    t_start = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        P = driver.time_integration(P, cfg, prm, rv, max_steps=1)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > budget:
+            break
+    tot = sum(times)
+    v = args.n * args.n * len(times) / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus,
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [args.n, args.n], "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": 1, "kind": "port",
+                         "sample": "%d steps of OT %dx%d (bounded to %.0f s)" % (len(times), args.n, args.n, budget)},
+        "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    from _cases import orszag_tang
+    from astronomix_gb300 import _native
+    from astronomix_gb300.time_integration import get_plan
+
+    dev_index = torch.cuda.current_device()
+    n = args.n
+    cfg, prm, rv, s = orszag_tang(n=n, t_end=1e9, dtype=np.float32)
+    p = _native.make_params(prm)
+    plan = get_plan(cfg, rv, s.shape, np.float32)
+    stream = torch.cuda.current_stream()
+    st = stream.cuda_stream
+    state = torch.from_numpy(s).cuda()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    plan.reset(st)
+
+    # warm-up: W steps, one launch each
+    for _ in range(max(args.warmup, 3)):
+        plan.run_async(state.data_ptr(), p, 1, st)
+    torch.cuda.synchronize()
+    it0 = plan.run(state.data_ptr(), p, 0, st)
+
+    K = args.steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(dev_index) as clk:
+        for i in range(K):
+            flush.zero_()
+            starts[i].record(stream)
+            plan.run_async(state.data_ptr(), p, 1, st)
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_s = sum(step_ms) / 1e3
+    it1 = plan.run(state.data_ptr(), p, 0, st)
+    k_mean = (it1.magnetic_iterations - it0.magnetic_iterations) / max(1, it1.steps - it0.steps)
+    status = it1.status
+    total_s_max = max_over_ranks(total_s, world)
+    value = world * n * n * K / total_s_max
+
+    # ---- fused multi-step throughput (K steps in one launch, L2-resident state)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    plan.run_async(state.data_ptr(), p, K, st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fused_ms = e0.elapsed_time(e1)
+
+    # ---- end to end through the C ABI with host buffers (pinned)
+    host = torch.from_numpy(s.copy()).pin_memory()
+    host_out = torch.empty_like(host).pin_memory()
+    dev2 = torch.empty_like(state)
+    nbytes = host.numel() * host.element_size()
+    Ke = max(10, min(K, 100))
+    es = [torch.cuda.Event(enable_timing=True) for _ in range(Ke)]
+    ee = [torch.cuda.Event(enable_timing=True) for _ in range(Ke)]
+    plan.reset(st)
+    for i in range(Ke):
+        flush.zero_()
+        es[i].record(stream)
+        dev2.copy_(host, non_blocking=True)
+        plan.run_async(dev2.data_ptr(), p, 1, st)
+        host_out.copy_(dev2, non_blocking=True)
+        ee[i].record(stream)
+    torch.cuda.synchronize()
+    e2e_s = sum(a.elapsed_time(b) for a, b in zip(es, ee)) / 1e3
+    e2e_s = max_over_ranks(e2e_s, world)
+    e2e_value = world * n * n * Ke / e2e_s
+
+    # ---- FP64: same kernels, plain double precision
+    cfg64, prm64, rv64, s64 = orszag_tang(n=n, t_end=1e9, dtype=np.float64)
+    plan64 = get_plan(cfg64, rv64, s64.shape, np.float64)
+    st64 = torch.from_numpy(s64).cuda()
+    plan64.reset(st)
+    for _ in range(3):
+        plan64.run_async(st64.data_ptr(), p, 1, st)
+    K64 = max(5, K // 10)
+    t64 = []
+    for _ in range(K64):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        plan64.run_async(st64.data_ptr(), p, 1, st)
+        b.record(stream)
+        t64.append((a, b))
+    torch.cuda.synchronize()
+    fp64_s = sum(a.elapsed_time(b) for a, b in t64) / 1e3
+    fp64_value = n * n * K64 / fp64_s
+
+    # ---- accuracy: FP32 vs FP64 density at t = 0.05 from the same initial state
+    t_cmp = 0.05
+    cfgA, prmA, rvA, sA = orszag_tang(n=n, t_end=t_cmp, dtype=np.float32)
+    cfgB, prmB, rvB, sB = orszag_tang(n=n, t_end=t_cmp, dtype=np.float64)
+    a32 = torch.from_numpy(sA).cuda()
+    a64 = torch.from_numpy(sB).cuda()
+    pa, pb = _native.make_params(prmA), _native.make_params(prmB)
+    planA = get_plan(cfgA, rvA, sA.shape, np.float32)
+    planB = get_plan(cfgB, rvB, sB.shape, np.float64)
+    planA.reset(st)
+    planB.reset(st)
+    infoA = planA.run(a32.data_ptr(), pa, 1 << 40, st)
+    infoB = planB.run(a64.data_ptr(), pb, 1 << 40, st)
+    r32 = a32[0].double()
+    r64 = a64[0]
+    l1 = float((r32 - r64).abs().sum() / r64.abs().sum())
+
+    # ---- roofline of the dominant (only) kernel: fv_run_kernel
+    bpz = algorithmic_bytes_per_zone_update(k_mean)
+    launch_s = total_s / K
+    achieved = bpz * n * n / launch_s / 1e9
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        peak, peak_src = 6800.0, "fallback"
+    traffic = load_traffic("fv_run_kernel_ot512_fp32_step")
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline_oracle()
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "zone-updates/s",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_s_max / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [n, n], "precision": "fp32 fields, fp64 dt/time",
+                   "l2": "flushed between timed steps (512 MB write); state 7.3 MB",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": e2e_value, "unit": "zone-updates/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "gpu_launches": K,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "note": "algorithmic %.0f B/zone-update (k=%.2f fixed-point iterations), peak %s" % (
+                         bpz, k_mean, peak_src)},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "fp64_value": fp64_value,
+        "fp32_over_fp64": value / fp64_value,
+        "l1_err_vs_fp64": l1,
+        "l1_t": t_cmp,
+        "l1_steps": [infoA.steps, infoB.steps],
+        "fused_multistep_value": n * n * K / (fused_ms / 1e3),
+        "magnetic_iterations_mean": k_mean,
+        "status": status,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        import torch
+
+        if not torch.cuda.is_available():
+            print(json.dumps({"metric": METRIC, "error": "no CUDA device"}))
+            sys.exit(1)
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
