@@ -112,6 +112,8 @@ SIGNATURES = {
     "amx_history": (_I32, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I32), _I64, _P]),
     "amx_conservation_sums": (_I32, [_P, _P, ctypes.POINTER(amx_params), ctypes.POINTER(_D), _P]),
     "amx_status": (_I32, [_P, ctypes.POINTER(_I32), _I32, _P]),
+    "amx_fv_run_noalloc": (_I32, [ctypes.POINTER(amx_config), _P, ctypes.POINTER(amx_params), _I64,
+                                  ctypes.POINTER(amx_run_info), _P]),
     "amx_version": (ctypes.c_char_p, []),
 }
 

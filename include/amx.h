@@ -192,6 +192,24 @@ int amx_conservation_sums(amx_plan* plan, const void* state, const amx_params* p
  * Synchronises the stream. */
 int amx_status(amx_plan* plan, int32_t* status_host, int32_t clear, void* stream);
 
+/* ---- allocation-free variant ----------------------------------------------- */
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory: a framework that owns the GPU's memory and forbids allocations
+ * behind its back (XLA preallocates most of the device; a JAX custom call
+ * must not take more), a process held to a fixed device-memory budget, or a
+ * loop that cannot afford an allocation's implicit synchronisation.  Runs
+ * `max_steps` FV time steps of `state` in place, like amx_run_async, without
+ * a plan.  Its scratch is a fixed 8 MiB __device__ array inside the library,
+ * shared by every call on a device (calls that overlap on the GPU race on
+ * it; each call clears what must start at zero); configurations that need
+ * more return AMX_ERR_TOO_LARGE (2D MHD fits up to 362^2 cells in FP32 and
+ * 255^2 in FP64; 3D MHD up to 49^3 / 39^3).  The first call on each device
+ * resolves the array's device address; make it before any stream capture.
+ * Fills *info (and synchronises) when info is non-null. */
+int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_params* prm, int64_t max_steps,
+                       amx_run_info* info, void* stream);
+
 /* Library version string. */
 const char* amx_version(void);
 
