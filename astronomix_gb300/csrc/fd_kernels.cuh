@@ -59,6 +59,21 @@ struct FDArgs {
   double t_pause;
 };
 
+// buffers and launch geometry handed from the host plan to the typed launchers
+struct FDLaunch {
+  int grid;        // blocks of the pointwise sweeps
+  int n;
+  void* bufs[10];  // Q0 Q QF QC ACC (8 rows) B BF (3) M (6) OM OB (3)
+  FDControl* ctl;
+};
+
+int fd_set_attrs_f32();
+int fd_set_attrs_f64();
+int fd_launch_stages_f32(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t s);
+int fd_launch_stages_f64(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t s);
+int fd_launch_cfl_f32(const FDLaunch& L, const void* state, const FDArgs& a, cudaStream_t s);
+int fd_launch_cfl_f64(const FDLaunch& L, const void* state, const FDArgs& a, cudaStream_t s);
+
 // ---------------------------------------------------------------- indexing
 
 __device__ __forceinline__ long long cidx(int i, int j, int k, int n) {
