@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 
@@ -206,6 +207,13 @@ int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out) 
       per_sm < 1) {
     amx_plan_destroy(p);
     return AMX_ERR_CUDA;
+  }
+  // AMX_FV_BLOCKS_PER_SM (optional) caps the resident blocks per SM of the
+  // persistent kernel: fewer blocks make the grid barrier cheaper, more hide
+  // latency better.
+  if (const char* env = std::getenv("AMX_FV_BLOCKS_PER_SM")) {
+    const int want = std::atoi(env);
+    if (want >= 1 && want < per_sm) per_sm = want;
   }
   const long long cap = (long long)per_sm * p->num_sms;
   const long long need = std::max<long long>(1, (p->ncells + amx::kFVThreads - 1) / amx::kFVThreads);

@@ -12,7 +12,10 @@
 // Each phase is a sweep over tiles; phases are separated by a bounded grid
 // barrier (amx_common.cuh), so the global reductions of the step (the CFL
 // maximum and the fixed-point residual of every magnetic iteration) never
-// leave the device.  A runtime `mode` runs a single seam instead of full
+// leave the device.  Every phase that writes the gas state also reduces the
+// maxima of |u_a| + c over what it wrote: that is the Lax-Friedrichs alpha of
+// the next stage and, after the last stage, the CFL estimate of the next
+// step, so neither needs a sweep of its own.  A runtime `mode` runs a single seam instead of full
 // steps, which is how the C-ABI exposes the reference's step-level functions.
 //
 // HBM layout: state[var][x][y][z] (C order, last axis contiguous), no ghost
@@ -26,8 +29,8 @@ namespace amx {
 
 // Control block in device memory (one per plan).
 struct FVControl {
-  unsigned long long cfl[3][4];   // [slot][axis] bitwise maxima of |u_a| + c
-  unsigned long long alpha[3][4]; // [slot][axis] Lax-Friedrichs alpha of a stage
+  unsigned long long red[3][4];   // [slot][axis] maxima of |u_a| + c of a state a phase wrote
+  unsigned long long spare[3][4];
   unsigned long long mag[3];      // [slot] fixed-point residual
   double dt;                      // dt of the last step taken
   double t;                       // simulation time
@@ -91,13 +94,13 @@ template <> struct Tile<float, 2> {
   static constexpr int T0 = 8, T1 = 64, T2 = 1;
 };
 template <> struct Tile<double, 2> {
-  static constexpr int T0 = 8, T1 = 32, T2 = 1;
+  static constexpr int T0 = 4, T1 = 64, T2 = 1;
 };
 template <> struct Tile<float, 3> {
-  static constexpr int T0 = 4, T1 = 8, T2 = 32;
+  static constexpr int T0 = 4, T1 = 4, T2 = 32;
 };
 template <> struct Tile<double, 3> {
-  static constexpr int T0 = 4, T1 = 4, T2 = 32;
+  static constexpr int T0 = 4, T1 = 4, T2 = 16;
 };
 
 constexpr int kFVThreads = 256;
@@ -110,11 +113,29 @@ struct TileGeom {
   static constexpr int HALO = H0 * H1 * H2;
   static constexpr int CELLS = T0 * T1 * T2;
   static constexpr int CPT = (CELLS + kFVThreads - 1) / kFVThreads;
+  // faces of one axis and the cells (tile +- 1 along the axis) whose slopes they use
   static constexpr int F0 = (T0 + 1) * T1 * T2;
   static constexpr int F1 = (DIM >= 2) ? T0 * (T1 + 1) * T2 : 0;
   static constexpr int F2 = (DIM >= 3) ? T0 * T1 * (T2 + 1) : 0;
   static constexpr int FMAX = F0 > F1 ? (F0 > F2 ? F0 : F2) : (F1 > F2 ? F1 : F2);
-  static constexpr size_t SMEM = sizeof(T) * (size_t)NV * (HALO + FMAX);
+  static constexpr int S0 = (T0 + 2) * T1 * T2;
+  static constexpr int S1 = (DIM >= 2) ? T0 * (T1 + 2) * T2 : 0;
+  static constexpr int S2 = (DIM >= 3) ? T0 * T1 * (T2 + 2) : 0;
+  static constexpr int SMAX = S0 > S1 ? (S0 > S2 ? S0 : S2) : (S1 > S2 ? S1 : S2);
+  // FUSED: all axes in one pass (slope and flux arrays side by side) instead
+  // of one axis at a time; measured slower on GB300 for both 2D and 3D
+  static constexpr bool FUSED = false;
+  // 3D (HBM-bound) precomputes the limited slopes once per cell; up to 2D
+  // (L2-resident, latency-bound) both faces evaluate them in registers
+  static constexpr bool SLOPES = DIM == 3;
+  static constexpr int SREG = SLOPES ? (FUSED ? S0 + S1 : SMAX) : 0;
+  static constexpr int FREG = FUSED ? F0 + F1 : FMAX;
+  // magnetic tile: halo 1, six values per cell (averaged B and E = B x v)
+  static constexpr int M0 = T0 + 2, M1 = (DIM >= 2) ? T1 + 2 : 1, M2 = (DIM >= 3) ? T2 + 2 : 1;
+  static constexpr int MHALO = M0 * M1 * M2;
+  static constexpr size_t HYDRO_SMEM = sizeof(T) * (size_t)NV * (HALO + FREG + SREG);
+  static constexpr size_t MAG_SMEM = sizeof(T) * (size_t)6 * MHALO;
+  static constexpr size_t SMEM = HYDRO_SMEM > MAG_SMEM ? HYDRO_SMEM : MAG_SMEM;
 };
 
 template <int DIM>
@@ -127,13 +148,11 @@ __host__ __device__ inline long long fv_num_tiles(int n, int T0, int T1, int T2)
 
 template <int DIM>
 __device__ __forceinline__ void tile_origin(long long tile, int n, int T0, int T1, int T2, int* o) {
-  const int n0 = (n + T0 - 1) / T0;
   const int n1 = (DIM >= 2) ? (n + T1 - 1) / T1 : 1;
   const int n2 = (DIM >= 3) ? (n + T2 - 1) / T2 : 1;
   const int t2 = (int)(tile % n2);
   const int t1 = (int)((tile / n2) % n1);
   const int t0 = (int)(tile / ((long long)n2 * n1));
-  (void)n0;
   o[0] = t0 * T0;
   o[1] = t1 * T1;
   o[2] = t2 * T2;
@@ -156,47 +175,40 @@ __device__ __forceinline__ int map_ax(const FVArgs<T>& a, int k, int g, bool* fl
   return map_index(g, n, a.bc[k], DIM == 1, flip);
 }
 
-// ------------------------------------------------------------ CFL phase
+// ------------------------------------------------------------ reductions
 
-// Per-axis maxima of |u_a| + c over all cells (the ghost cells of the
-// reference are copies of interior cells and add nothing to the maximum).
-template <typename T, int DIM>
-__device__ __noinline__ void phase_cfl(const FVArgs<T>& a, unsigned long long* slot, double* red) {
-  const T gamma = T(a.gamma);
-  T m[3] = {T(0), T(0), T(0)};
-  const long long nc = a.ncells;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (long long)gridDim.x * blockDim.x) {
-    const T rho = a.state[c];
-    const T p = a.state[(DIM + 1) * nc + c];
-    const T cs = sound_speed(rho, p, gamma);
-#pragma unroll
-    for (int k = 0; k < DIM; ++k) m[k] = nanmax(m[k], Num<T>::abs_(a.state[(1 + k) * nc + c]) + cs);
-  }
+// Folds per-thread maxima of |u_a| + c into `slot` (block max + atomicMax).
+template <int DIM>
+__device__ __forceinline__ void fold_maxima(const double* m, unsigned long long* slot, double* red) {
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
-    const double r = block_max<double>((double)m[k], red);
+    const double r = block_max<double>(m[k], red);
     if (threadIdx.x == 0) atomic_max_nonneg(&slot[k], r);
   }
 }
 
-// Lax-Friedrichs alpha of a stage input (max over cells of |u_d| + c).
 template <typename T, int DIM>
-__device__ __noinline__ void phase_alpha(const FVArgs<T>& a, const T* P, unsigned long long* slot, double* red) {
+__device__ __forceinline__ void track_maxima(const T* q, T gamma, double* m) {
+  const T cs = sound_speed(q[0], q[DIM + 1], gamma);
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) m[k] = nanmax(m[k], (double)(Num<T>::abs_(q[1 + k]) + cs));
+}
+
+// Per-axis maxima of |u_a| + c over all cells of the state (the reference's
+// ghost cells are copies of interior cells and add nothing to the maximum).
+template <typename T, int DIM>
+__device__ __noinline__ void phase_cfl(const FVArgs<T>& a, unsigned long long* slot, double* red) {
   const T gamma = T(a.gamma);
-  T m[3] = {T(0), T(0), T(0)};
+  double m[3] = {0.0, 0.0, 0.0};
   const long long nc = a.ncells;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
        c += (long long)gridDim.x * blockDim.x) {
-    const T cs = sound_speed(P[c], P[(DIM + 1) * nc + c], gamma);
+    T q[DIM + 2];
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) m[k] = nanmax(m[k], Num<T>::abs_(P[(1 + k) * nc + c]) + cs);
+    for (int v = 0; v < DIM + 2; ++v) q[v] = a.state[v * nc + c];
+    track_maxima<T, DIM>(q, gamma, m);
   }
-#pragma unroll
-  for (int k = 0; k < DIM; ++k) {
-    const double r = block_max<double>((double)m[k], red);
-    if (threadIdx.x == 0) atomic_max_nonneg(&slot[k], r);
-  }
+  fold_maxima<DIM>(m, slot, red);
 }
 
 // ------------------------------------------------------------ hydro stage
@@ -206,10 +218,14 @@ __device__ __noinline__ void phase_alpha(const FVArgs<T>& a, const T* P, unsigne
 //   P_out = prim(U)
 // and, when `P0` is given, the RK2 combination of evolve_state.py:456-469:
 //   P_out = prim(0.5 (cons(P0) + cons(prim(U)))).
-// `alpha` holds the Lax-Friedrichs alpha per axis (unused otherwise).
+// `alpha` holds the Lax-Friedrichs alpha per axis (unused otherwise).  The
+// limited slope of every cell (reconstruction.py:399-431) is computed once
+// per axis into shared memory and read by both of its faces.  The maxima of
+// |u_a| + c of P_out are folded into `out_slot`.
 template <typename T, int DIM, int RS>
 __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __restrict__ Pin, T* Pout,
-                                  const T* P0, T dt, const T* alpha, T* smem) {
+                                               const T* P0, T dt, const T* alpha, T* smem,
+                                               unsigned long long* out_slot, double* red) {
   using G = TileGeom<T, DIM>;
   constexpr int NV = G::NV;
   const int n = a.n;
@@ -217,9 +233,11 @@ __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __re
   const T gamma = T(a.gamma);
   const T dxT = T(a.dx);
   const T inv_dx = T(1.0 / a.dx);
-  T* sP = smem;                      // [NV][HALO]
-  T* sF = smem + NV * G::HALO;       // [NV][FMAX]
+  T* sP = smem;                        // [NV][HALO]
+  T* sF = smem + NV * G::HALO;         // [NV][FMAX]
+  T* sD = sF + NV * G::FMAX;           // [NV][SMAX] slopes (already * dx / 2)
   const long long ntiles = fv_num_tiles<DIM>(n, G::T0, G::T1, G::T2);
+  double m[3] = {0.0, 0.0, 0.0};
 
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int o[3];
@@ -259,31 +277,72 @@ __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __re
       }
     }
 
-    // ---- axes in the reference order x, y, z
+    // ---- axes in the reference order x, y, z.  Fused (DIM <= 2): slopes of
+    // all axes, one barrier, fluxes of all axes, one barrier, then every cell
+    // adds its x and then its y flux differences.  3D: one axis at a time.
+    constexpr int NPASS = G::FUSED ? 1 : DIM;
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) {
-      const int E0 = G::T0 + (k == 0), E1 = (DIM >= 2) ? G::T1 + (k == 1) : 1, E2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
-      const int nf = E0 * E1 * E2;
-      const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
-      for (int f = threadIdx.x; f < nf; f += blockDim.x) {
-        const int f2 = f % E2, f1 = (f / E2) % E1, f0 = f / (E2 * E1);
-        // halo index of the cell right of the face (local cell c = face index)
-        const int h = ((f0 + 2) * G::H1 + (DIM >= 2 ? f1 + 2 : 0)) * G::H2 + (DIM >= 3 ? f2 + 2 : 0);
-        T qL[NV], qR[NV];
+    for (int pass = 0; pass < NPASS; ++pass) {
+      const int k_lo = G::FUSED ? 0 : pass, k_hi = G::FUSED ? DIM : pass + 1;
+      for (int k = k_lo; k < (G::SLOPES ? k_hi : k_lo); ++k) {
+        const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
+        const int D0 = G::T0 + 2 * (k == 0), D1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1,
+                  D2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
+        const int ns = D0 * D1 * D2;
+        T* sDk = sD + ((G::FUSED && k == 1) ? NV * G::S0 : 0);
+        const int sdim = G::FUSED ? (k == 0 ? G::S0 : G::S1) : G::SMAX;
+        for (int e = threadIdx.x; e < ns; e += blockDim.x) {
+          const int d2 = e % D2, d1 = (e / D2) % D1, d0 = e / (D2 * D1);
+          const int h = ((d0 + 2 - (k == 0)) * G::H1 + (DIM >= 2 ? d1 + 2 - (k == 1) : 0)) * G::H2 +
+                        (DIM >= 3 ? d2 + 2 - (k == 2) : 0);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          const T* s = sP + v * G::HALO + h;
-          const T qm2 = s[-2 * stride], qm1 = s[-stride], q0 = s[0], qp1 = s[stride];
-          const T gm1 = limited((qm1 - qm2) / dxT, (q0 - qm1) / dxT, a.limiter, dxT);
-          const T g0 = limited((q0 - qm1) / dxT, (qp1 - q0) / dxT, a.limiter, dxT);
-          qL[v] = qm1 + gm1 * dxT / T(2);
-          qR[v] = q0 - g0 * dxT / T(2);
+          for (int v = 0; v < NV; ++v) {
+            const T* s = sP + v * G::HALO + h;
+            const T qm = s[-stride], q0 = s[0], qp = s[stride];
+            sDk[v * sdim + e] = limited((q0 - qm) / dxT, (qp - q0) / dxT, a.limiter, dxT) * dxT / T(2);
+          }
         }
-        T F[NV];
-        riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), a.lm != 0, F);
-        // face f stored at its own (E0,E1,E2) index
+      }
+      if (G::SLOPES) __syncthreads();
+      for (int k = k_lo; k < k_hi; ++k) {
+        const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
+        const int D1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1, D2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
+        const T* sDk = sD + ((G::FUSED && k == 1) ? NV * G::S0 : 0);
+        const int sdim = G::FUSED ? (k == 0 ? G::S0 : G::S1) : G::SMAX;
+        T* sFk = sF + ((G::FUSED && k == 1) ? NV * G::F0 : 0);
+        const int fdim = G::FUSED ? (k == 0 ? G::F0 : G::F1) : G::FMAX;
+        const int E0 = G::T0 + (k == 0), E1 = (DIM >= 2) ? G::T1 + (k == 1) : 1,
+                  E2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
+        const int nf = E0 * E1 * E2;
+        const int dstride = (k == 0) ? D1 * D2 : ((k == 1) ? D2 : 1);
+        for (int f = threadIdx.x; f < nf; f += blockDim.x) {
+          const int f2 = f % E2, f1 = (f / E2) % E1, f0 = f / (E2 * E1);
+          // halo index of the cell right of the face (local cell c = face index)
+          const int h = ((f0 + 2) * G::H1 + (DIM >= 2 ? f1 + 2 : 0)) * G::H2 + (DIM >= 3 ? f2 + 2 : 0);
+          // slope index of that cell (slope arrays start one cell before the tile along k)
+          const int ds = (f0 + (k == 0)) * D1 * D2 + (DIM >= 2 ? (f1 + (k == 1)) * D2 : 0) +
+                         (DIM >= 3 ? f2 + (k == 2) : 0);
+          T qL[NV], qR[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) sF[v * G::FMAX + f] = F[v];
+          for (int v = 0; v < NV; ++v) {
+            const T* s = sP + v * G::HALO + h;
+            if (G::SLOPES) {
+              const T* d = sDk + v * sdim + ds;
+              qL[v] = s[-stride] + d[-dstride];
+              qR[v] = s[0] - d[0];
+            } else {
+              const T qm2 = s[-2 * stride], qm1 = s[-stride], q0 = s[0], qp1 = s[stride];
+              const T gm1 = limited((qm1 - qm2) / dxT, (q0 - qm1) / dxT, a.limiter, dxT);
+              const T g0 = limited((q0 - qm1) / dxT, (qp1 - q0) / dxT, a.limiter, dxT);
+              qL[v] = qm1 + gm1 * dxT / T(2);
+              qR[v] = q0 - g0 * dxT / T(2);
+            }
+          }
+          T F[NV];
+          riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), a.lm != 0, F);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) sFk[v * fdim + f] = F[v];
+        }
       }
       __syncthreads();
 #pragma unroll
@@ -291,14 +350,19 @@ __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __re
         const int cl = threadIdx.x + j * kFVThreads;
         if (cl < G::CELLS) {
           const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
-          const int fl = (c0 * E1 + c1) * E2 + c2;  // face i-1/2 of the cell
-          const int fr = fl + ((k == 0) ? E1 * E2 : ((k == 1) ? E2 : 1));
+          for (int k = k_lo; k < k_hi; ++k) {
+            const T* sFk = sF + ((G::FUSED && k == 1) ? NV * G::F0 : 0);
+            const int fdim = G::FUSED ? (k == 0 ? G::F0 : G::F1) : G::FMAX;
+            const int E1 = (DIM >= 2) ? G::T1 + (k == 1) : 1, E2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
+            const int fl = (c0 * E1 + c1) * E2 + c2;  // face i-1/2 of the cell
+            const int fr = fl + ((k == 0) ? E1 * E2 : ((k == 1) ? E2 : 1));
 #pragma unroll
-          for (int v = 0; v < NV; ++v)
-            U[j][v] = U[j][v] + inv_dx * (sF[v * G::FMAX + fl] - sF[v * G::FMAX + fr]) * dt;
+            for (int v = 0; v < NV; ++v)
+              U[j][v] = U[j][v] + inv_dx * (sFk[v * fdim + fl] - sFk[v * fdim + fr]) * dt;
+          }
         }
       }
-      __syncthreads();
+      if (!G::FUSED) __syncthreads();
     }
 
     // ---- back to primitives (+ RK2 combination) and store
@@ -324,14 +388,23 @@ __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __re
           }
 #pragma unroll
           for (int v = 0; v < NV; ++v) Pout[v * nc + c] = q[v];
+          if (out_slot) track_maxima<T, DIM>(q, gamma, m);
         }
       }
     }
-    __syncthreads();
+    if (G::FUSED) __syncthreads();  // the flux arrays are read above; the next tile overwrites them
   }
+  if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
 
 // ------------------------------------------------------------ magnetic sub-step
+
+template <typename T>
+__device__ __forceinline__ void cross3(const T* a, const T* b, T* r) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
 
 // Loads the 3-vectors B and v at a (boundary-mapped) cell.  `Bs`/`vs` are
 // either the iterate buffer (6 rows) or, for the first evaluation, the
@@ -353,13 +426,6 @@ __device__ __forceinline__ void load_Bv(const MagSrc<T, DIM>& s, long long c, lo
   v[2] = (DIM == 2 && s.from_gas) ? T(0) : s.v[2 * nc + c];
 }
 
-template <typename T>
-__device__ __forceinline__ void cross3(const T* a, const T* b, T* r) {
-  r[0] = a[1] * b[2] - a[2] * b[1];
-  r[1] = a[2] * b[0] - a[0] * b[2];
-  r[2] = a[0] * b[1] - a[1] * b[0];
-}
-
 template <typename T, int DIM>
 __device__ __forceinline__ long long mag_neighbor(const FVArgs<T>& a, const int* ic, int k, int off) {
   int j[3] = {ic[0], ic[1], ic[2]};
@@ -368,11 +434,12 @@ __device__ __forceinline__ long long mag_neighbor(const FVArgs<T>& a, const int*
   return cell_index<DIM>(j[0], j[1], j[2], a.n);
 }
 
-// One evaluation of the fixed-point map (_magnetic_field_update.py:82-105,
-// :143-165): writes B_{k+1}, v_{k+1} to `dst` and folds max |B_k - B_{k+1}|,
-// max |v_k - v_{k+1}| into `slot`.
+// One evaluation of the fixed-point map without shared memory: every cell
+// gathers the averaged fields of its 2*DIM neighbours itself (L1 serves the
+// reuse).  Used when the state is L2-resident (2D), where the tiled variant
+// below loses more to tile imbalance and barriers than it saves in loads.
 template <typename T, int DIM>
-__device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, MagSrc<T, DIM> src, T* dst, T dt,
+__device__ __noinline__ void phase_mag_iterate_direct(const FVArgs<T>& a, MagSrc<T, DIM> src, T* dst, T dt,
                                   unsigned long long* slot, double* red) {
   const long long nc = a.ncells;
   const int n = a.n;
@@ -455,11 +522,133 @@ __device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, MagSrc<T, DIM
   if (threadIdx.x == 0) atomic_max_nonneg(slot, r);
 }
 
-// Pressure refresh with gamma = 5/3 and write-back (_magnetic_field_update.py:208-242).
+// B and v iterates: `Bk`/`vk` are the iterate buffer rows, or null for the
+// first evaluation, which starts from B0 and v0 (the state's B rows and gas
+// velocity, vz = 0 in 2D as in _magnetic_field_update.py:60-70).
 template <typename T, int DIM>
-__device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* Bv) {
+__device__ __forceinline__ void load_iter(const FVArgs<T>& a, const T* src, long long c, long long nc, T* Bk,
+                                          T* vk, T* B0, T* v0) {
+  const T* st = a.state;
+  B0[0] = st[(DIM + 2) * nc + c];
+  B0[1] = st[(DIM + 3) * nc + c];
+  B0[2] = st[(DIM + 4) * nc + c];
+  v0[0] = st[nc + c];
+  v0[1] = st[2 * nc + c];
+  v0[2] = (DIM == 3) ? st[3 * nc + c] : T(0);
+  if (src) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { Bk[i] = src[i * nc + c]; vk[i] = src[(3 + i) * nc + c]; }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { Bk[i] = B0[i]; vk[i] = v0[i]; }
+  }
+}
+
+// One evaluation of the fixed-point map (_magnetic_field_update.py:82-105,
+// :143-165): B_{k+1} = B0 - dt curl(B x v), v_{k+1} = v0 - dt (B x curl B)/rho
+// with B, v the averages (midpoint) or the iterate (Euler).  A halo-1 tile of
+// the averaged B and of E = B x v is staged in shared memory, so every cell
+// computes its cross product once.  Folds max |B_k - B_{k+1}| and
+// max |v_k - v_{k+1}| into `slot`.
+template <typename T, int DIM>
+__device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, const T* src, T* dst, T dt,
+                                               unsigned long long* slot, double* red, T* smem) {
+  using G = TileGeom<T, DIM>;
+  const long long nc = a.ncells;
+  const int n = a.n;
+  const T dx = T(a.dx);
+  const bool midpoint = (a.integrator == 0);
+  T* sB = smem;                 // [3][MHALO] averaged B
+  T* sE = smem + 3 * G::MHALO;  // [3][MHALO] E = B x v
+  const long long ntiles = fv_num_tiles<DIM>(n, G::T0, G::T1, G::T2);
+  T change = T(0);
+
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int o[3];
+    tile_origin<DIM>(tile, n, G::T0, G::T1, G::T2, o);
+    for (int e = threadIdx.x; e < G::MHALO; e += blockDim.x) {
+      const int h2 = e % G::M2, h1 = (e / G::M2) % G::M1, h0 = e / (G::M2 * G::M1);
+      bool fl = false;
+      const int i0 = map_ax<T, DIM>(a, 0, o[0] + h0 - 1, &fl);
+      const int i1 = map_ax<T, DIM>(a, 1, o[1] + h1 - 1, &fl);
+      const int i2 = (DIM >= 3) ? map_ax<T, DIM>(a, 2, o[2] + h2 - 1, &fl) : 0;
+      const long long c = cell_index<DIM>(i0, i1, i2, n);
+      T Bk[3], vk[3], B0[3], v0[3], Ba[3], va[3], E[3];
+      load_iter<T, DIM>(a, src, c, nc, Bk, vk, B0, v0);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        Ba[i] = midpoint ? (Bk[i] + B0[i]) / T(2) : Bk[i];
+        va[i] = midpoint ? (vk[i] + v0[i]) / T(2) : vk[i];
+      }
+      cross3(Ba, va, E);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) { sB[i * G::MHALO + e] = Ba[i]; sE[i * G::MHALO + e] = E[i]; }
+    }
+    __syncthreads();
+    for (int cl = threadIdx.x; cl < G::CELLS; cl += blockDim.x) {
+      const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
+      const int g0 = o[0] + c0, g1 = o[1] + c1, g2 = o[2] + c2;
+      if (g0 >= n || g1 >= n || (DIM >= 3 && g2 >= n)) continue;
+      const long long c = cell_index<DIM>(g0, g1, g2, n);
+      const int h = ((c0 + 1) * G::M1 + (c1 + 1)) * G::M2 + (DIM >= 3 ? c2 + 1 : 0);
+      const int st[3] = {G::M1 * G::M2, G::M2, 1};
+      // d(F_i)/d(x_k) = 0.5 (F_i[+] - F_i[-]) / dx  (_vector_maths.py:55-100)
+      auto dF = [&](const T* F, int i, int k) {
+        return T(0.5) * (F[i * G::MHALO + h + st[k]] - F[i * G::MHALO + h - st[k]]) / dx;
+      };
+      T curlE[3], curlB[3];
+      if (DIM == 2) {
+        curlE[0] = dF(sE, 2, 1);
+        curlE[1] = -dF(sE, 2, 0);
+        curlE[2] = dF(sE, 1, 0) - dF(sE, 0, 1);
+        curlB[0] = dF(sB, 2, 1);
+        curlB[1] = -dF(sB, 2, 0);
+        curlB[2] = dF(sB, 1, 0) - dF(sB, 0, 1);
+      } else {
+        curlE[0] = dF(sE, 2, 1) - dF(sE, 1, 2);
+        curlE[1] = dF(sE, 0, 2) - dF(sE, 2, 0);
+        curlE[2] = dF(sE, 1, 0) - dF(sE, 0, 1);
+        curlB[0] = dF(sB, 2, 1) - dF(sB, 1, 2);
+        curlB[1] = dF(sB, 0, 2) - dF(sB, 2, 0);
+        curlB[2] = dF(sB, 1, 0) - dF(sB, 0, 1);
+      }
+      T Bk[3], vk[3], B0[3], v0[3], Ba[3];
+      load_iter<T, DIM>(a, src, c, nc, Bk, vk, B0, v0);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Ba[i] = sB[i * G::MHALO + h];
+      T phi2[3];
+      cross3(Ba, curlB, phi2);
+      const T r = a.state[c];
+      T Bn[3], vn[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        Bn[i] = B0[i] - dt * curlE[i];
+        vn[i] = v0[i] - dt * (phi2[i] / r);
+      }
+      const T dB = Num<T>::sqrt_(sq(Bk[0] - Bn[0]) + sq(Bk[1] - Bn[1]) + sq(Bk[2] - Bn[2]));
+      const T dv = Num<T>::sqrt_(sq(vk[0] - vn[0]) + sq(vk[1] - vn[1]) + sq(vk[2] - vn[2]));
+      change = nanmax(change, nanmax(dB, dv));
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        dst[i * nc + c] = Bn[i];
+        dst[(3 + i) * nc + c] = vn[i];
+      }
+    }
+    __syncthreads();
+  }
+  const double r = block_max<double>((double)change, red);
+  if (threadIdx.x == 0) atomic_max_nonneg(slot, r);
+}
+
+// Pressure refresh with gamma = 5/3 and write-back (_magnetic_field_update.py:208-242);
+// folds the maxima of |u_a| + c of the updated gas into `out_slot`.
+template <typename T, int DIM>
+__device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* Bv, unsigned long long* out_slot,
+                                                double* red) {
   const long long nc = a.ncells;
   const T g53 = T(5.0 / 3.0);
+  const T gamma = T(a.gamma);
+  double m[3] = {0.0, 0.0, 0.0};
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
        c += (long long)gridDim.x * blockDim.x) {
     const T rho = a.state[c];
@@ -476,12 +665,20 @@ __device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* Bv)
     T E = total_energy(rho, v0abs, p, g53);
     E = E - T(0.5) * rho * (v0abs * v0abs) + T(0.5) * rho * (vnabs * vnabs);
     const T pn = pressure_from_energy(E, rho, vnabs, g53);
+    T q[DIM + 2];
+    q[0] = rho;
 #pragma unroll
-    for (int i = 0; i < DIM; ++i) a.state[(1 + i) * nc + c] = vn[i];
+    for (int i = 0; i < DIM; ++i) {
+      a.state[(1 + i) * nc + c] = vn[i];
+      q[1 + i] = vn[i];
+    }
     a.state[(DIM + 1) * nc + c] = pn;
+    q[DIM + 1] = pn;
 #pragma unroll
     for (int i = 0; i < 3; ++i) a.state[(DIM + 2 + i) * nc + c] = Bn[i];
+    if (out_slot) track_maxima<T, DIM>(q, gamma, m);
   }
+  if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
 
 // ------------------------------------------------------------ the kernel
@@ -499,36 +696,53 @@ fv_run_kernel(FVArgs<T> a) {
   T* gas = a.state;
   __shared__ T s_alpha[3];
 
-  int cfl_pass = 0, mag_pass = 0, lf_pass = 0;
+  // Producer ring of maxima: the phase with pass number rp writes slot rp % 3
+  // after block 0 cleared slot (rp + 1) % 3; the slot a phase reads is the
+  // one written by the previous producer, (rp - 1) % 3.
+  int rp = 0, mag_pass = 0;
 
-  // LF alpha of a stage input; returns false on a barrier failure
-  auto stage_alpha = [&](const T* P) -> bool {
-    if (RS != RS_LF) return true;
-    unsigned long long* slot = ctl->alpha[lf_pass % 3];
-    phase_alpha<T, DIM>(a, P, slot, red);
-    if (!grid_sync(bar, status)) return false;
-    if (threadIdx.x < DIM) s_alpha[threadIdx.x] = T(bits_to_double(slot[threadIdx.x]));
-    if (blockIdx.x == 0 && threadIdx.x < 4) ctl->alpha[(lf_pass + 2) % 3][threadIdx.x] = 0ull;
-    __syncthreads();
-    ++lf_pass;
-    return true;
+  auto produce_slot = [&]() -> unsigned long long* {
+    if (blockIdx.x == 0 && threadIdx.x < 4) ctl->red[(rp + 1) % 3][threadIdx.x] = 0ull;
+    return ctl->red[rp % 3];
   };
-
-  // one RK2 update of the gas rows with stage dt `h` (evolve_state.py:419-488)
-  auto rk2 = [&](T h) -> bool {
-    if (!stage_alpha(gas)) return false;
-    phase_hydro_stage<T, DIM, RS>(a, gas, a.p1, nullptr, h, RS == RS_LF ? s_alpha : nullptr, smem);
-    if (!grid_sync(bar, status)) return false;
-    if (!stage_alpha(a.p1)) return false;
-    phase_hydro_stage<T, DIM, RS>(a, a.p1, gas, gas, h, RS == RS_LF ? s_alpha : nullptr, smem);
+  auto last_maxima = [&](double* m) {
+    volatile unsigned long long* s = ctl->red[(rp + 2) % 3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) m[k] = (k < DIM) ? bits_to_double(s[k]) : 0.0;
+  };
+  auto set_alpha = [&]() {
+    if (RS != RS_LF) return;
+    double m[3];
+    last_maxima(m);
+    if (threadIdx.x < DIM) s_alpha[threadIdx.x] = T(m[threadIdx.x]);
+    __syncthreads();
+  };
+  // `need`: whether anything reads the maxima of this stage's output (the
+  // next stage's Lax-Friedrichs alpha, or the next step's dt)
+  auto stage = [&](const T* in, T* out, const T* p0, T h, bool need) -> bool {
+    set_alpha();
+    unsigned long long* slot = produce_slot();
+    phase_hydro_stage<T, DIM, RS>(a, in, out, p0, h, RS == RS_LF ? s_alpha : nullptr, smem,
+                                  (need || RS == RS_LF) ? slot : nullptr, red);
+    ++rp;
     return grid_sync(bar, status);
+  };
+  // one RK2 update of the gas rows with stage dt `h` (evolve_state.py:419-488);
+  // `last`: the update ends the time step
+  auto rk2 = [&](T h, bool last) -> bool {
+    if (!stage(gas, a.p1, nullptr, h, false)) return false;
+    return stage(a.p1, gas, gas, h, last);
   };
 
   // magnetic_update (_magnetic_field_update.py:37-242); returns iterations or -1
   auto magnetic = [&](T h) -> int {
-    const MagSrc<T, DIM> first{gas + (DIM + 2) * nc, gas + nc, true};
     unsigned long long* slot = &ctl->mag[mag_pass % 3];
-    phase_mag_iterate<T, DIM>(a, first, a.mag0, h, slot, red);
+    if (DIM == 2) {
+      const MagSrc<T, DIM> first{gas + (DIM + 2) * nc, gas + nc, true};
+      phase_mag_iterate_direct<T, DIM>(a, first, a.mag0, h, slot, red);
+    } else {
+      phase_mag_iterate<T, DIM>(a, nullptr, a.mag0, h, slot, red, smem);
+    }
     if (!grid_sync(bar, status)) return -1;
     double change = bits_to_double(*(volatile unsigned long long*)slot);
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->mag[(mag_pass + 2) % 3] = 0ull;
@@ -537,9 +751,13 @@ fv_run_kernel(FVArgs<T> a) {
     T* cur = a.mag0;
     T* nxt = a.mag1;
     while (change > a.tol && it < a.max_iters) {
-      const MagSrc<T, DIM> src{cur, cur + 3 * nc, false};
       slot = &ctl->mag[mag_pass % 3];
-      phase_mag_iterate<T, DIM>(a, src, nxt, h, slot, red);
+      if (DIM == 2) {
+        const MagSrc<T, DIM> src{cur, cur + 3 * nc, false};
+        phase_mag_iterate_direct<T, DIM>(a, src, nxt, h, slot, red);
+      } else {
+        phase_mag_iterate<T, DIM>(a, cur, nxt, h, slot, red, smem);
+      }
       if (!grid_sync(bar, status)) return -1;
       change = bits_to_double(*(volatile unsigned long long*)slot);
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->mag[(mag_pass + 2) % 3] = 0ull;
@@ -549,35 +767,39 @@ fv_run_kernel(FVArgs<T> a) {
     }
     if (change > a.tol && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_NOT_CONVERGED);
     if (change != change && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_NAN);
-    phase_mag_finalize<T, DIM>(a, cur);
+    unsigned long long* out = produce_slot();
+    phase_mag_finalize<T, DIM>(a, cur, RS == RS_LF ? out : nullptr, red);
+    ++rp;
     if (!grid_sync(bar, status)) return -1;
     return it;
   };
 
-  auto cfl = [&](double* dt_out) -> bool {
-    unsigned long long* slot = ctl->cfl[cfl_pass % 3];
-    phase_cfl<T, DIM>(a, slot, red);
-    if (!grid_sync(bar, status)) return false;
+  // CFL dt from the maxima of the last producer (_timestep_estimator.py:118-128)
+  auto dt_from_maxima = [&]() -> double {
+    double m[3];
+    last_maxima(m);
     double sum = 0.0;
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) {
-      const double m = bits_to_double(*(volatile unsigned long long*)&slot[k]);
-      sum = (k == 0) ? m / a.dx : sum + m / a.dx;
-    }
-    *dt_out = a.C_cfl * 1.0 / sum;
-    if (blockIdx.x == 0 && threadIdx.x < 4) ctl->cfl[(cfl_pass + 2) % 3][threadIdx.x] = 0ull;
-    ++cfl_pass;
-    return true;
+    for (int k = 0; k < DIM; ++k) sum = (k == 0) ? m[k] / a.dx : sum + m[k] / a.dx;
+    return a.C_cfl * 1.0 / sum;
+  };
+  auto cfl_phase = [&]() -> bool {
+    unsigned long long* slot = produce_slot();
+    phase_cfl<T, DIM>(a, slot, red);
+    ++rp;
+    return grid_sync(bar, status);
   };
 
   if (a.mode == FV_MODE_CFL) {
-    double dt;
-    if (!cfl(&dt)) return;
+    if (!cfl_phase()) return;
+    const double dt = dt_from_maxima();
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->dt = dt;
     return;
   }
+  // the seams need the maxima of the state they start from (Lax-Friedrichs alpha)
   if (a.mode == FV_MODE_HYDRO_RK2) {
-    rk2(T(a.dt_in * a.dt_scale));
+    if (!cfl_phase()) return;
+    rk2(T(a.dt_in * a.dt_scale), false);
     return;
   }
   if (a.mode == FV_MODE_MAGNETIC) {
@@ -587,15 +809,16 @@ fv_run_kernel(FVArgs<T> a) {
     return;
   }
   if (a.mode == FV_MODE_EVOLVE) {
+    if (!cfl_phase()) return;
     const T dtT = T(a.dt_in);
     if (MHD) {
-      if (!rk2(dtT / T(2))) return;
+      if (!rk2(dtT / T(2), false)) return;
       const int it = magnetic(dtT);
       if (it < 0) return;
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->mag_iters = it;
-      rk2(dtT / T(2));
+      rk2(dtT / T(2), false);
     } else {
-      rk2(dtT);
+      rk2(dtT, false);
     }
     return;
   }
@@ -603,7 +826,7 @@ fv_run_kernel(FVArgs<T> a) {
   // ---- full time steps (time_integration.py:386-762)
   const long long step0 = *(volatile long long*)&ctl->steps;
   double t = *(volatile double*)&ctl->t;
-  if (!grid_sync(bar, status)) return;  // everyone has read t before it changes
+  if (!cfl_phase()) return;  // also orders everyone's read of t before it changes
   for (long long s = 0; s < a.max_steps; ++s) {
     double dt;
     if (t >= a.t_pause) break;
@@ -611,18 +834,18 @@ fv_run_kernel(FVArgs<T> a) {
       dt = a.dt_fixed;
     } else {
       if (!(t < a.t_end)) break;
-      if (!cfl(&dt)) return;
+      dt = dt_from_maxima();
     }
     if (a.exact_end_time) dt = fmin(dt, a.t_end - t);
     const T dtT = T(dt);
     int it = 0;
     if (MHD) {
-      if (!rk2(dtT / T(2))) return;
+      if (!rk2(dtT / T(2), false)) return;
       it = magnetic(dtT);
       if (it < 0) return;
-      if (!rk2(dtT / T(2))) return;
+      if (!rk2(dtT / T(2), true)) return;
     } else {
-      if (!rk2(dtT)) return;
+      if (!rk2(dtT, true)) return;
     }
     t = t + dt;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
