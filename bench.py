@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CELLS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-arena", action="store_true", help="skip the 256^3 blast comparison")
     return ap.parse_args()
 
 
@@ -129,6 +130,75 @@ class ClockSampler:
         reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.samples)}
+
+
+# The reference's own published benchmark: 3D MHD blast (arena/arena_tests/mhd/
+# blast_test1.py:1-160), rho = 1, p = 100 inside r0 = 0.125 with a linear ramp
+# to p = 1 at r1 = 1.1 r0, B = 10 (1, 1, 0)/sqrt(2), FP32, on 1x H200:
+# fd_mhd 0.771 s/step and fv_mhd 0.0564 s/step at 256^3 (arena/*.svg).
+H200_S_PER_STEP = {"fd": 0.771, "fv": 0.0564}
+
+
+def arena_blast(n, solver):
+    from astronomix_gb300 import (SimulationConfig, SimulationParams, get_registered_variables, finalize_config,
+                                  construct_primitive_state, initialize_interface_fields, FINITE_DIFFERENCE,
+                                  FINITE_VOLUME, LAX_FRIEDRICHS, PERIODIC_ROLL, SINGLE_PRECISION)
+    from _cases import PERIODIC_2D
+
+    if solver == "fd":
+        cfg = SimulationConfig(solver_mode=FINITE_DIFFERENCE, mhd=True, dimensionality=3, num_cells=n,
+                               boundary_handling=PERIODIC_ROLL, boundary_settings=PERIODIC_2D)
+        prm = SimulationParams(C_cfl=1.5, minimum_density=1e-3, minimum_pressure=1e-3, t_end=0.02)
+    else:
+        cfg = SimulationConfig(solver_mode=FINITE_VOLUME, numerical_precision=SINGLE_PRECISION, mhd=True,
+                               dimensionality=3, num_cells=n, riemann_solver=LAX_FRIEDRICHS,
+                               boundary_handling=PERIODIC_ROLL, boundary_settings=PERIODIC_2D)
+        prm = SimulationParams(C_cfl=0.8, t_end=0.02)
+    rv = get_registered_variables(cfg)
+    x = (np.arange(n) + 0.5) / n
+    X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
+    r = np.sqrt((X - 0.5) ** 2 + (Y - 0.5) ** 2 + (Z - 0.5) ** 2)
+    r0, r1 = 0.125, 1.1 * 0.125
+    P = np.where(r <= r0, 100.0, np.where(r <= r1, 1.0 + 99.0 * (r1 - r) / (r1 - r0), 1.0))
+    z = np.zeros_like(r, dtype=np.float32)
+    b = np.full_like(z, 10 / np.sqrt(2))
+    kw = dict(density=np.ones_like(z), velocity_x=z, velocity_y=z, velocity_z=z, magnetic_field_x=b,
+              magnetic_field_y=b, magnetic_field_z=z, gas_pressure=P)
+    if solver == "fd":
+        fx, fy, fz = initialize_interface_fields(b, b, z)
+        kw.update(interface_magnetic_field_x=fx, interface_magnetic_field_y=fy, interface_magnetic_field_z=fz)
+    s = construct_primitive_state(cfg, rv, **kw)
+    cfg = finalize_config(cfg, s.shape)
+    return cfg, prm, rv, s
+
+
+def time_arena(solver, n=256, steps=3):
+    """s/step of the reference's published blast benchmark on this GPU (state > L2)."""
+    import torch
+    from astronomix_gb300 import _native
+    from astronomix_gb300.time_integration import get_plan
+
+    cfg, prm, rv, s = arena_blast(n, solver)
+    plan = get_plan(cfg, rv, s.shape, np.float32)
+    p = _native.make_params(prm)
+    st = torch.cuda.current_stream()
+    dev = torch.from_numpy(s).cuda()
+    plan.reset(st.cuda_stream)
+    plan.run_async(dev.data_ptr(), p, 2, st.cuda_stream)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    plan.run_async(dev.data_ptr(), p, steps, st.cuda_stream)
+    b.record(st)
+    torch.cuda.synchronize()
+    info = plan.run(dev.data_ptr(), p, 0, st.cuda_stream)
+    sps = a.elapsed_time(b) / 1e3 / steps
+    ok = bool(torch.isfinite(dev).all()) and info.status == 0
+    del dev
+    return {"grid": [n, n, n], "s_per_step": sps, "zone_updates_per_s": n ** 3 / sps,
+            "h200_published_s_per_step": H200_S_PER_STEP[solver],
+            "speedup_vs_h200_published": H200_S_PER_STEP[solver] / sps, "finite": ok,
+            "steps_timed": steps}
 
 
 def algorithmic_bytes_per_zone_update(k_mean, elem=4):
@@ -239,8 +309,10 @@ def run_ours(args, rank, world):
     it1 = plan.run(state.data_ptr(), p, 0, st)
     k_mean = (it1.magnetic_iterations - it0.magnetic_iterations) / max(1, it1.steps - it0.steps)
     status = it1.status
+    from astronomix_gb300.replicas import replica_throughput
+
+    value = replica_throughput(n * n * K, total_s)
     total_s_max = max_over_ranks(total_s, world)
-    value = world * n * n * K / total_s_max
 
     # ---- fused multi-step throughput (K steps in one launch, L2-resident state)
     torch.cuda.synchronize()
@@ -269,8 +341,7 @@ def run_ours(args, rank, world):
         ee[i].record(stream)
     torch.cuda.synchronize()
     e2e_s = sum(a.elapsed_time(b) for a, b in zip(es, ee)) / 1e3
-    e2e_s = max_over_ranks(e2e_s, world)
-    e2e_value = world * n * n * Ke / e2e_s
+    e2e_value = replica_throughput(n * n * Ke, e2e_s)
 
     # ---- FP64: same kernels, plain double precision
     cfg64, prm64, rv64, s64 = orszag_tang(n=n, t_end=1e9, dtype=np.float64)
@@ -322,6 +393,10 @@ def run_ours(args, rank, world):
         peak, peak_src = 6800.0, "fallback"
     traffic = load_traffic("fv_run_kernel_ot512_fp32_step")
 
+    arena = {}
+    if not args.no_arena:
+        arena = {"fd_blast_fp32": time_arena("fd"), "fv_lf_blast_fp32": time_arena("fv")}
+
     if rank != 0:
         return
     cpu = None
@@ -359,6 +434,7 @@ def run_ours(args, rank, world):
         "l1_steps": [infoA.steps, infoB.steps],
         "fused_multistep_value": n * n * K / (fused_ms / 1e3),
         "magnetic_iterations_mean": k_mean,
+        "reference_published_workloads": arena,
         "status": status,
     }
     print(json.dumps(line))
