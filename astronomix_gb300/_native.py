@@ -114,6 +114,19 @@ SIGNATURES = {
     "amx_status": (_I32, [_P, ctypes.POINTER(_I32), _I32, _P]),
     "amx_fv_run_noalloc": (_I32, [ctypes.POINTER(amx_config), _P, ctypes.POINTER(amx_params), _I64,
                                   ctypes.POINTER(amx_run_info), _P]),
+    "amx_batch_create": (_I32, [ctypes.POINTER(amx_config), _I32, ctypes.POINTER(_I32), ctypes.POINTER(_D),
+                                ctypes.POINTER(_P)]),
+    "amx_batch_destroy": (_I32, [_P]),
+    "amx_batch_workspace_bytes": (_I32, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    "amx_batch_reset": (_I32, [_P, _P]),
+    "amx_batch_run": (_I32, [_P, ctypes.POINTER(_P), ctypes.POINTER(amx_params), ctypes.POINTER(_D), _I64, _I32,
+                             _P]),
+    "amx_batch_info": (_I32, [_P, ctypes.POINTER(amx_run_info), ctypes.POINTER(_I64), _P]),
+    "amx_batch_tune": (_I32, [_P, ctypes.POINTER(_P), ctypes.POINTER(amx_params), ctypes.POINTER(_D), _I32,
+                              ctypes.POINTER(_D), _P]),
+    "amx_batch_tiling": (_I32, [_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I32),
+                                ctypes.POINTER(_I32)]),
+    "amx_batch_set_tiling": (_I32, [_P, _I32, _I32]),
     "amx_version": (ctypes.c_char_p, []),
 }
 
@@ -234,3 +247,69 @@ class Plan:
         st = ctypes.c_int32()
         check(self._L.amx_status(self.handle, ctypes.byref(st), int(bool(clear)), _P(stream)), "amx_status")
         return st.value
+
+
+class Batch:
+    """Owns an ``amx_batch``: device workspace and launch state of an ensemble
+    of 2D FV runs sharing one template configuration."""
+
+    def __init__(self, tmpl: amx_config, num_cells, box_size):
+        self._L = lib()
+        self.num_runs = len(num_cells)
+        n = (ctypes.c_int32 * self.num_runs)(*[int(v) for v in num_cells])
+        b = (ctypes.c_double * self.num_runs)(*[float(v) for v in box_size])
+        h = ctypes.c_void_p()
+        check(self._L.amx_batch_create(ctypes.byref(tmpl), self.num_runs, n, b, ctypes.byref(h)), "amx_batch_create")
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self._L.amx_batch_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def _ptrs(self, state_ptrs):
+        if len(state_ptrs) != self.num_runs:
+            raise ValueError("expected %d state pointers, got %d" % (self.num_runs, len(state_ptrs)))
+        return (ctypes.c_void_p * self.num_runs)(*[int(p) for p in state_ptrs])
+
+    def _t_end(self, t_end):
+        if len(t_end) != self.num_runs:
+            raise ValueError("expected %d end times, got %d" % (self.num_runs, len(t_end)))
+        return (ctypes.c_double * self.num_runs)(*[float(t) for t in t_end])
+
+    def workspace_bytes(self) -> int:
+        n = ctypes.c_size_t()
+        check(self._L.amx_batch_workspace_bytes(self.handle, ctypes.byref(n)))
+        return n.value
+
+    def reset(self, stream=0):
+        check(self._L.amx_batch_reset(self.handle, _P(stream)), "amx_batch_reset")
+
+    def run(self, state_ptrs, prm: amx_params, t_end, max_steps, use_graph=True, stream=0):
+        check(self._L.amx_batch_run(self.handle, self._ptrs(state_ptrs), ctypes.byref(prm), self._t_end(t_end),
+                                    int(max_steps), int(bool(use_graph)), _P(stream)), "amx_batch_run")
+
+    def info(self, stream=0):
+        infos = (amx_run_info * self.num_runs)()
+        lock = ctypes.c_int64()
+        check(self._L.amx_batch_info(self.handle, infos, ctypes.byref(lock), _P(stream)), "amx_batch_info")
+        return list(infos), lock.value
+
+    def tune(self, state_ptrs, prm: amx_params, t_end, steps=3, stream=0) -> float:
+        best = ctypes.c_double()
+        check(self._L.amx_batch_tune(self.handle, self._ptrs(state_ptrs), ctypes.byref(prm), self._t_end(t_end),
+                                     int(steps), ctypes.byref(best), _P(stream)), "amx_batch_tune")
+        return best.value
+
+    def tiling(self):
+        v, b, t0, t1 = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        check(self._L.amx_batch_tiling(self.handle, ctypes.byref(v), ctypes.byref(b), ctypes.byref(t0),
+                                       ctypes.byref(t1)), "amx_batch_tiling")
+        return {"variant": v.value, "blocks_per_sm": b.value, "tile": (t0.value, t1.value)}
+
+    def set_tiling(self, variant, blocks_per_sm=0):
+        check(self._L.amx_batch_set_tiling(self.handle, int(variant), int(blocks_per_sm)), "amx_batch_set_tiling")

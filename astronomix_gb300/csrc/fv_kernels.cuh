@@ -103,12 +103,22 @@ template <> struct Tile<double, 3> {
   static constexpr int T0 = 4, T1 = 4, T2 = 16;
 };
 
+// Alternative tile shapes the batched driver's autotuner chooses from
+// (variant 0 is Tile<T, DIM>).
+template <typename T, int DIM, int V> struct TileV : Tile<T, DIM> {};
+template <typename T> struct TileV<T, 2, 1> {
+  static constexpr int T0 = 4, T1 = 64, T2 = 1;
+};
+template <typename T> struct TileV<T, 2, 2> {
+  static constexpr int T0 = 16, T1 = 32, T2 = 1;
+};
+
 constexpr int kFVThreads = 256;
 
-template <typename T, int DIM>
+template <typename T, int DIM, int V = 0>
 struct TileGeom {
   static constexpr int NV = DIM + 2;
-  static constexpr int T0 = Tile<T, DIM>::T0, T1 = Tile<T, DIM>::T1, T2 = Tile<T, DIM>::T2;
+  static constexpr int T0 = TileV<T, DIM, V>::T0, T1 = TileV<T, DIM, V>::T1, T2 = TileV<T, DIM, V>::T2;
   static constexpr int H0 = T0 + 4, H1 = (DIM >= 2) ? T1 + 4 : 1, H2 = (DIM >= 3) ? T2 + 4 : 1;
   static constexpr int HALO = H0 * H1 * H2;
   static constexpr int CELLS = T0 * T1 * T2;
@@ -222,11 +232,10 @@ __device__ __noinline__ void phase_cfl(const FVArgs<T>& a, unsigned long long* s
 // limited slope of every cell (reconstruction.py:399-431) is computed once
 // per axis into shared memory and read by both of its faces.  The maxima of
 // |u_a| + c of P_out are folded into `out_slot`.
-template <typename T, int DIM, int RS>
-__device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __restrict__ Pin, T* Pout,
-                                               const T* P0, T dt, const T* alpha, T* smem,
-                                               unsigned long long* out_slot, double* red) {
-  using G = TileGeom<T, DIM>;
+template <typename T, int DIM, int RS, int V = 0>
+__device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, const T* __restrict__ Pin, T* Pout,
+                                           const T* P0, T dt, const T* alpha, T* smem, double* m, bool track) {
+  using G = TileGeom<T, DIM, V>;
   constexpr int NV = G::NV;
   const int n = a.n;
   const long long nc = a.ncells;
@@ -236,163 +245,170 @@ __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __re
   T* sP = smem;                        // [NV][HALO]
   T* sF = smem + NV * G::HALO;         // [NV][FMAX]
   T* sD = sF + NV * G::FMAX;           // [NV][SMAX] slopes (already * dx / 2)
-  const long long ntiles = fv_num_tiles<DIM>(n, G::T0, G::T1, G::T2);
-  double m[3] = {0.0, 0.0, 0.0};
 
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    int o[3];
-    tile_origin<DIM>(tile, n, G::T0, G::T1, G::T2, o);
-
-    // ---- load the halo'd tile of primitives (boundary-mapped)
-    for (int e = threadIdx.x; e < G::HALO; e += blockDim.x) {
-      const int h2 = e % G::H2;
-      const int h1 = (e / G::H2) % G::H1;
-      const int h0 = e / (G::H2 * G::H1);
-      bool f0 = false, f1 = false, f2 = false;
-      const int i0 = map_ax<T, DIM>(a, 0, o[0] + h0 - 2, &f0);
-      const int i1 = (DIM >= 2) ? map_ax<T, DIM>(a, 1, o[1] + h1 - 2, &f1) : 0;
-      const int i2 = (DIM >= 3) ? map_ax<T, DIM>(a, 2, o[2] + h2 - 2, &f2) : 0;
-      const long long c = cell_index<DIM>(i0, i1, i2, n);
+  // ---- load the halo'd tile of primitives (boundary-mapped)
+  for (int e = threadIdx.x; e < G::HALO; e += blockDim.x) {
+    const int h2 = e % G::H2;
+    const int h1 = (e / G::H2) % G::H1;
+    const int h0 = e / (G::H2 * G::H1);
+    bool f0 = false, f1 = false, f2 = false;
+    const int i0 = map_ax<T, DIM>(a, 0, o[0] + h0 - 2, &f0);
+    const int i1 = (DIM >= 2) ? map_ax<T, DIM>(a, 1, o[1] + h1 - 2, &f1) : 0;
+    const int i2 = (DIM >= 3) ? map_ax<T, DIM>(a, 2, o[2] + h2 - 2, &f2) : 0;
+    const long long c = cell_index<DIM>(i0, i1, i2, n);
 #pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        T val = Pin[v * nc + c];
-        if ((v == 1 && f0) || (v == 2 && f1) || (v == 3 && f2)) val = -val;
-        sP[v * G::HALO + e] = val;
+    for (int v = 0; v < NV; ++v) {
+      T val = Pin[v * nc + c];
+      if ((v == 1 && f0) || (v == 2 && f1) || (v == 3 && f2)) val = -val;
+      sP[v * G::HALO + e] = val;
+    }
+  }
+  __syncthreads();
+
+  // ---- per-thread cells: conserved state from the (mapped) primitives
+  T U[G::CPT][NV];
+#pragma unroll
+  for (int j = 0; j < G::CPT; ++j) {
+    const int cl = threadIdx.x + j * kFVThreads;
+    if (cl < G::CELLS) {
+      const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
+      const int h = ((c0 + 2) * G::H1 + (DIM >= 2 ? c1 + 2 : 0)) * G::H2 + (DIM >= 3 ? c2 + 2 : 0);
+      T q[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) q[v] = sP[v * G::HALO + h];
+      prim_to_cons<T, DIM>(q, U[j], gamma);
+    }
+  }
+
+  // ---- axes in the reference order x, y, z.  Fused (DIM <= 2): slopes of
+  // all axes, one barrier, fluxes of all axes, one barrier, then every cell
+  // adds its x and then its y flux differences.  3D: one axis at a time.
+  constexpr int NPASS = G::FUSED ? 1 : DIM;
+#pragma unroll
+  for (int pass = 0; pass < NPASS; ++pass) {
+    const int k_lo = G::FUSED ? 0 : pass, k_hi = G::FUSED ? DIM : pass + 1;
+    for (int k = k_lo; k < (G::SLOPES ? k_hi : k_lo); ++k) {
+      const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
+      const int D0 = G::T0 + 2 * (k == 0), D1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1,
+                D2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
+      const int ns = D0 * D1 * D2;
+      T* sDk = sD + ((G::FUSED && k == 1) ? NV * G::S0 : 0);
+      const int sdim = G::FUSED ? (k == 0 ? G::S0 : G::S1) : G::SMAX;
+      for (int e = threadIdx.x; e < ns; e += blockDim.x) {
+        const int d2 = e % D2, d1 = (e / D2) % D1, d0 = e / (D2 * D1);
+        const int h = ((d0 + 2 - (k == 0)) * G::H1 + (DIM >= 2 ? d1 + 2 - (k == 1) : 0)) * G::H2 +
+                      (DIM >= 3 ? d2 + 2 - (k == 2) : 0);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const T* s = sP + v * G::HALO + h;
+          const T qm = s[-stride], q0 = s[0], qp = s[stride];
+          sDk[v * sdim + e] = limited((q0 - qm) / dxT, (qp - q0) / dxT, a.limiter, dxT) * dxT / T(2);
+        }
+      }
+    }
+    if (G::SLOPES) __syncthreads();
+    for (int k = k_lo; k < k_hi; ++k) {
+      const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
+      const int D1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1, D2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
+      const T* sDk = sD + ((G::FUSED && k == 1) ? NV * G::S0 : 0);
+      const int sdim = G::FUSED ? (k == 0 ? G::S0 : G::S1) : G::SMAX;
+      T* sFk = sF + ((G::FUSED && k == 1) ? NV * G::F0 : 0);
+      const int fdim = G::FUSED ? (k == 0 ? G::F0 : G::F1) : G::FMAX;
+      const int E0 = G::T0 + (k == 0), E1 = (DIM >= 2) ? G::T1 + (k == 1) : 1,
+                E2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
+      const int nf = E0 * E1 * E2;
+      const int dstride = (k == 0) ? D1 * D2 : ((k == 1) ? D2 : 1);
+      for (int f = threadIdx.x; f < nf; f += blockDim.x) {
+        const int f2 = f % E2, f1 = (f / E2) % E1, f0 = f / (E2 * E1);
+        // halo index of the cell right of the face (local cell c = face index)
+        const int h = ((f0 + 2) * G::H1 + (DIM >= 2 ? f1 + 2 : 0)) * G::H2 + (DIM >= 3 ? f2 + 2 : 0);
+        // slope index of that cell (slope arrays start one cell before the tile along k)
+        const int ds = (f0 + (k == 0)) * D1 * D2 + (DIM >= 2 ? (f1 + (k == 1)) * D2 : 0) +
+                       (DIM >= 3 ? f2 + (k == 2) : 0);
+        T qL[NV], qR[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const T* s = sP + v * G::HALO + h;
+          if (G::SLOPES) {
+            const T* d = sDk + v * sdim + ds;
+            qL[v] = s[-stride] + d[-dstride];
+            qR[v] = s[0] - d[0];
+          } else {
+            const T qm2 = s[-2 * stride], qm1 = s[-stride], q0 = s[0], qp1 = s[stride];
+            const T gm1 = limited((qm1 - qm2) / dxT, (q0 - qm1) / dxT, a.limiter, dxT);
+            const T g0 = limited((q0 - qm1) / dxT, (qp1 - q0) / dxT, a.limiter, dxT);
+            qL[v] = qm1 + gm1 * dxT / T(2);
+            qR[v] = q0 - g0 * dxT / T(2);
+          }
+        }
+        T F[NV];
+        riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), a.lm != 0, F);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) sFk[v * fdim + f] = F[v];
       }
     }
     __syncthreads();
-
-    // ---- per-thread cells: conserved state from the (mapped) primitives
-    T U[G::CPT][NV];
 #pragma unroll
     for (int j = 0; j < G::CPT; ++j) {
       const int cl = threadIdx.x + j * kFVThreads;
       if (cl < G::CELLS) {
         const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
-        const int h = ((c0 + 2) * G::H1 + (DIM >= 2 ? c1 + 2 : 0)) * G::H2 + (DIM >= 3 ? c2 + 2 : 0);
+        for (int k = k_lo; k < k_hi; ++k) {
+          const T* sFk = sF + ((G::FUSED && k == 1) ? NV * G::F0 : 0);
+          const int fdim = G::FUSED ? (k == 0 ? G::F0 : G::F1) : G::FMAX;
+          const int E1 = (DIM >= 2) ? G::T1 + (k == 1) : 1, E2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
+          const int fl = (c0 * E1 + c1) * E2 + c2;  // face i-1/2 of the cell
+          const int fr = fl + ((k == 0) ? E1 * E2 : ((k == 1) ? E2 : 1));
+#pragma unroll
+          for (int v = 0; v < NV; ++v)
+            U[j][v] = U[j][v] + inv_dx * (sFk[v * fdim + fl] - sFk[v * fdim + fr]) * dt;
+        }
+      }
+    }
+    if (!G::FUSED) __syncthreads();
+  }
+
+  // ---- back to primitives (+ RK2 combination) and store
+#pragma unroll
+  for (int j = 0; j < G::CPT; ++j) {
+    const int cl = threadIdx.x + j * kFVThreads;
+    if (cl < G::CELLS) {
+      const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
+      const int g0 = o[0] + c0, g1 = o[1] + c1, g2 = o[2] + c2;
+      if (g0 < n && (DIM < 2 || g1 < n) && (DIM < 3 || g2 < n)) {
+        const long long c = cell_index<DIM>(g0, g1, g2, n);
         T q[NV];
+        cons_to_prim<T, DIM>(U[j], q, gamma);
+        if (P0) {
+          T U2[NV], q0[NV], U0[NV];
+          prim_to_cons<T, DIM>(q, U2, gamma);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) q[v] = sP[v * G::HALO + h];
-        prim_to_cons<T, DIM>(q, U[j], gamma);
+          for (int v = 0; v < NV; ++v) q0[v] = P0[v * nc + c];
+          prim_to_cons<T, DIM>(q0, U0, gamma);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) U2[v] = T(0.5) * (U0[v] + U2[v]);
+          cons_to_prim<T, DIM>(U2, q, gamma);
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) Pout[v * nc + c] = q[v];
+        if (track) track_maxima<T, DIM>(q, gamma, m);
       }
     }
+  }
+  if (G::FUSED) __syncthreads();  // the flux arrays are read above; the next tile overwrites them
+}
 
-    // ---- axes in the reference order x, y, z.  Fused (DIM <= 2): slopes of
-    // all axes, one barrier, fluxes of all axes, one barrier, then every cell
-    // adds its x and then its y flux differences.  3D: one axis at a time.
-    constexpr int NPASS = G::FUSED ? 1 : DIM;
-#pragma unroll
-    for (int pass = 0; pass < NPASS; ++pass) {
-      const int k_lo = G::FUSED ? 0 : pass, k_hi = G::FUSED ? DIM : pass + 1;
-      for (int k = k_lo; k < (G::SLOPES ? k_hi : k_lo); ++k) {
-        const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
-        const int D0 = G::T0 + 2 * (k == 0), D1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1,
-                  D2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
-        const int ns = D0 * D1 * D2;
-        T* sDk = sD + ((G::FUSED && k == 1) ? NV * G::S0 : 0);
-        const int sdim = G::FUSED ? (k == 0 ? G::S0 : G::S1) : G::SMAX;
-        for (int e = threadIdx.x; e < ns; e += blockDim.x) {
-          const int d2 = e % D2, d1 = (e / D2) % D1, d0 = e / (D2 * D1);
-          const int h = ((d0 + 2 - (k == 0)) * G::H1 + (DIM >= 2 ? d1 + 2 - (k == 1) : 0)) * G::H2 +
-                        (DIM >= 3 ? d2 + 2 - (k == 2) : 0);
-#pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            const T* s = sP + v * G::HALO + h;
-            const T qm = s[-stride], q0 = s[0], qp = s[stride];
-            sDk[v * sdim + e] = limited((q0 - qm) / dxT, (qp - q0) / dxT, a.limiter, dxT) * dxT / T(2);
-          }
-        }
-      }
-      if (G::SLOPES) __syncthreads();
-      for (int k = k_lo; k < k_hi; ++k) {
-        const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
-        const int D1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1, D2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
-        const T* sDk = sD + ((G::FUSED && k == 1) ? NV * G::S0 : 0);
-        const int sdim = G::FUSED ? (k == 0 ? G::S0 : G::S1) : G::SMAX;
-        T* sFk = sF + ((G::FUSED && k == 1) ? NV * G::F0 : 0);
-        const int fdim = G::FUSED ? (k == 0 ? G::F0 : G::F1) : G::FMAX;
-        const int E0 = G::T0 + (k == 0), E1 = (DIM >= 2) ? G::T1 + (k == 1) : 1,
-                  E2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
-        const int nf = E0 * E1 * E2;
-        const int dstride = (k == 0) ? D1 * D2 : ((k == 1) ? D2 : 1);
-        for (int f = threadIdx.x; f < nf; f += blockDim.x) {
-          const int f2 = f % E2, f1 = (f / E2) % E1, f0 = f / (E2 * E1);
-          // halo index of the cell right of the face (local cell c = face index)
-          const int h = ((f0 + 2) * G::H1 + (DIM >= 2 ? f1 + 2 : 0)) * G::H2 + (DIM >= 3 ? f2 + 2 : 0);
-          // slope index of that cell (slope arrays start one cell before the tile along k)
-          const int ds = (f0 + (k == 0)) * D1 * D2 + (DIM >= 2 ? (f1 + (k == 1)) * D2 : 0) +
-                         (DIM >= 3 ? f2 + (k == 2) : 0);
-          T qL[NV], qR[NV];
-#pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            const T* s = sP + v * G::HALO + h;
-            if (G::SLOPES) {
-              const T* d = sDk + v * sdim + ds;
-              qL[v] = s[-stride] + d[-dstride];
-              qR[v] = s[0] - d[0];
-            } else {
-              const T qm2 = s[-2 * stride], qm1 = s[-stride], q0 = s[0], qp1 = s[stride];
-              const T gm1 = limited((qm1 - qm2) / dxT, (q0 - qm1) / dxT, a.limiter, dxT);
-              const T g0 = limited((q0 - qm1) / dxT, (qp1 - q0) / dxT, a.limiter, dxT);
-              qL[v] = qm1 + gm1 * dxT / T(2);
-              qR[v] = q0 - g0 * dxT / T(2);
-            }
-          }
-          T F[NV];
-          riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), a.lm != 0, F);
-#pragma unroll
-          for (int v = 0; v < NV; ++v) sFk[v * fdim + f] = F[v];
-        }
-      }
-      __syncthreads();
-#pragma unroll
-      for (int j = 0; j < G::CPT; ++j) {
-        const int cl = threadIdx.x + j * kFVThreads;
-        if (cl < G::CELLS) {
-          const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
-          for (int k = k_lo; k < k_hi; ++k) {
-            const T* sFk = sF + ((G::FUSED && k == 1) ? NV * G::F0 : 0);
-            const int fdim = G::FUSED ? (k == 0 ? G::F0 : G::F1) : G::FMAX;
-            const int E1 = (DIM >= 2) ? G::T1 + (k == 1) : 1, E2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
-            const int fl = (c0 * E1 + c1) * E2 + c2;  // face i-1/2 of the cell
-            const int fr = fl + ((k == 0) ? E1 * E2 : ((k == 1) ? E2 : 1));
-#pragma unroll
-            for (int v = 0; v < NV; ++v)
-              U[j][v] = U[j][v] + inv_dx * (sFk[v * fdim + fl] - sFk[v * fdim + fr]) * dt;
-          }
-        }
-      }
-      if (!G::FUSED) __syncthreads();
-    }
-
-    // ---- back to primitives (+ RK2 combination) and store
-#pragma unroll
-    for (int j = 0; j < G::CPT; ++j) {
-      const int cl = threadIdx.x + j * kFVThreads;
-      if (cl < G::CELLS) {
-        const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
-        const int g0 = o[0] + c0, g1 = o[1] + c1, g2 = o[2] + c2;
-        if (g0 < n && (DIM < 2 || g1 < n) && (DIM < 3 || g2 < n)) {
-          const long long c = cell_index<DIM>(g0, g1, g2, n);
-          T q[NV];
-          cons_to_prim<T, DIM>(U[j], q, gamma);
-          if (P0) {
-            T U2[NV], q0[NV], U0[NV];
-            prim_to_cons<T, DIM>(q, U2, gamma);
-#pragma unroll
-            for (int v = 0; v < NV; ++v) q0[v] = P0[v * nc + c];
-            prim_to_cons<T, DIM>(q0, U0, gamma);
-#pragma unroll
-            for (int v = 0; v < NV; ++v) U2[v] = T(0.5) * (U0[v] + U2[v]);
-            cons_to_prim<T, DIM>(U2, q, gamma);
-          }
-#pragma unroll
-          for (int v = 0; v < NV; ++v) Pout[v * nc + c] = q[v];
-          if (out_slot) track_maxima<T, DIM>(q, gamma, m);
-        }
-      }
-    }
-    if (G::FUSED) __syncthreads();  // the flux arrays are read above; the next tile overwrites them
+template <typename T, int DIM, int RS>
+__device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __restrict__ Pin, T* Pout,
+                                               const T* P0, T dt, const T* alpha, T* smem,
+                                               unsigned long long* out_slot, double* red) {
+  using G = TileGeom<T, DIM>;
+  const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
+  double m[3] = {0.0, 0.0, 0.0};
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int o[3];
+    tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
+    hydro_tile<T, DIM, RS>(a, o, Pin, Pout, P0, dt, alpha, smem, m, out_slot != nullptr);
   }
   if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
@@ -439,85 +455,95 @@ __device__ __forceinline__ long long mag_neighbor(const FVArgs<T>& a, const int*
 // reuse).  Used when the state is L2-resident (2D), where the tiled variant
 // below loses more to tile imbalance and barriers than it saves in loads.
 template <typename T, int DIM>
-__device__ __noinline__ void phase_mag_iterate_direct(const FVArgs<T>& a, MagSrc<T, DIM> src, T* dst, T dt,
-                                  unsigned long long* slot, double* red) {
+__device__ __forceinline__ void mag_direct_cell(const FVArgs<T>& a, const MagSrc<T, DIM>& src, T* dst, T dt,
+                                                long long c, T& change) {
   const long long nc = a.ncells;
   const int n = a.n;
   const T dx = T(a.dx);
   const MagSrc<T, DIM> s0{a.state + (DIM + 2) * nc, a.state + nc, true};  // B0, v0
   const T* rho = a.state;
   const bool midpoint = (a.integrator == 0);
+  int ic[3];
+  if (DIM == 2) { ic[0] = (int)(c / n); ic[1] = (int)(c % n); ic[2] = 0; }
+  else { ic[2] = (int)(c % n); ic[1] = (int)((c / n) % n); ic[0] = (int)(c / ((long long)n * n)); }
+  // averaged fields at the cell and its 2*DIM neighbours
+  T Bc[3], vc[3], B0c[3], v0c[3];
+  auto avg_at = [&](long long cc, T* Ba, T* va, T* Bk_out, T* vk_out, T* B0_out, T* v0_out) {
+    T Bk[3], vk[3], B0[3], v0[3];
+    load_Bv<T, DIM>(src, cc, nc, Bk, vk);
+    load_Bv<T, DIM>(s0, cc, nc, B0, v0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (midpoint) { Ba[i] = (Bk[i] + B0[i]) / T(2); va[i] = (vk[i] + v0[i]) / T(2); }
+      else { Ba[i] = Bk[i]; va[i] = vk[i]; }
+      if (Bk_out) { Bk_out[i] = Bk[i]; vk_out[i] = vk[i]; B0_out[i] = B0[i]; v0_out[i] = v0[i]; }
+    }
+  };
+  T Ba_c[3], va_c[3];
+  avg_at(c, Ba_c, va_c, Bc, vc, B0c, v0c);
+  // E = cross(B, v) and B at neighbours; curls by central differences
+  T Ep[3][3], Em[3][3], Bp[3][3], Bm[3][3];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    T Ba[3], va[3];
+    avg_at(mag_neighbor<T, DIM>(a, ic, k, +1), Ba, va, nullptr, nullptr, nullptr, nullptr);
+    cross3(Ba, va, Ep[k]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) Bp[k][i] = Ba[i];
+    avg_at(mag_neighbor<T, DIM>(a, ic, k, -1), Ba, va, nullptr, nullptr, nullptr, nullptr);
+    cross3(Ba, va, Em[k]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) Bm[k][i] = Ba[i];
+  }
+  // d(F_i)/d(x_k) = 0.5 (F_i[+] - F_i[-]) / dx
+  auto dF = [&](T (*Fp)[3], T (*Fm)[3], int i, int k) { return T(0.5) * (Fp[k][i] - Fm[k][i]) / dx; };
+  T curlE[3], curlB[3];
+  if (DIM == 2) {
+    curlE[0] = dF(Ep, Em, 2, 1);
+    curlE[1] = -dF(Ep, Em, 2, 0);
+    curlE[2] = dF(Ep, Em, 1, 0) - dF(Ep, Em, 0, 1);
+    curlB[0] = dF(Bp, Bm, 2, 1);
+    curlB[1] = -dF(Bp, Bm, 2, 0);
+    curlB[2] = dF(Bp, Bm, 1, 0) - dF(Bp, Bm, 0, 1);
+  } else {
+    curlE[0] = dF(Ep, Em, 2, 1) - dF(Ep, Em, 1, 2);
+    curlE[1] = dF(Ep, Em, 0, 2) - dF(Ep, Em, 2, 0);
+    curlE[2] = dF(Ep, Em, 1, 0) - dF(Ep, Em, 0, 1);
+    curlB[0] = dF(Bp, Bm, 2, 1) - dF(Bp, Bm, 1, 2);
+    curlB[1] = dF(Bp, Bm, 0, 2) - dF(Bp, Bm, 2, 0);
+    curlB[2] = dF(Bp, Bm, 1, 0) - dF(Bp, Bm, 0, 1);
+  }
+  T phi2[3];
+  cross3(Ba_c, curlB, phi2);
+  const T r = rho[c];
+  T Bn[3], vn[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Bn[i] = B0c[i] - dt * curlE[i];
+    vn[i] = v0c[i] - dt * (phi2[i] / r);
+  }
+  const T dB = Num<T>::sqrt_(sq(Bc[0] - Bn[0]) + sq(Bc[1] - Bn[1]) + sq(Bc[2] - Bn[2]));
+  const T dv = Num<T>::sqrt_(sq(vc[0] - vn[0]) + sq(vc[1] - vn[1]) + sq(vc[2] - vn[2]));
+  change = nanmax(change, nanmax(dB, dv));
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    dst[i * nc + c] = Bn[i];
+    dst[(3 + i) * nc + c] = vn[i];
+  }
+}
+
+// One evaluation of the fixed-point map without shared memory: every cell
+// gathers the averaged fields of its 2*DIM neighbours itself (L1 serves the
+// reuse).  Used when the state is L2-resident (2D), where the tiled variant
+// below loses more to tile imbalance and barriers than it saves in loads.
+template <typename T, int DIM>
+__device__ __noinline__ void phase_mag_iterate_direct(const FVArgs<T>& a, MagSrc<T, DIM> src, T* dst, T dt,
+                                  unsigned long long* slot, double* red) {
+  const long long nc = a.ncells;
   T change = T(0);
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (long long)gridDim.x * blockDim.x) {
-    int ic[3];
-    if (DIM == 2) { ic[0] = (int)(c / n); ic[1] = (int)(c % n); ic[2] = 0; }
-    else { ic[2] = (int)(c % n); ic[1] = (int)((c / n) % n); ic[0] = (int)(c / ((long long)n * n)); }
-    // averaged fields at the cell and its 2*DIM neighbours
-    T Bc[3], vc[3], B0c[3], v0c[3];
-    auto avg_at = [&](long long cc, T* Ba, T* va, T* Bk_out, T* vk_out, T* B0_out, T* v0_out) {
-      T Bk[3], vk[3], B0[3], v0[3];
-      load_Bv<T, DIM>(src, cc, nc, Bk, vk);
-      load_Bv<T, DIM>(s0, cc, nc, B0, v0);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        if (midpoint) { Ba[i] = (Bk[i] + B0[i]) / T(2); va[i] = (vk[i] + v0[i]) / T(2); }
-        else { Ba[i] = Bk[i]; va[i] = vk[i]; }
-        if (Bk_out) { Bk_out[i] = Bk[i]; vk_out[i] = vk[i]; B0_out[i] = B0[i]; v0_out[i] = v0[i]; }
-      }
-    };
-    T Ba_c[3], va_c[3];
-    avg_at(c, Ba_c, va_c, Bc, vc, B0c, v0c);
-    // E = cross(B, v) and B at neighbours; curls by central differences
-    T Ep[3][3], Em[3][3], Bp[3][3], Bm[3][3];
-#pragma unroll
-    for (int k = 0; k < DIM; ++k) {
-      T Ba[3], va[3];
-      avg_at(mag_neighbor<T, DIM>(a, ic, k, +1), Ba, va, nullptr, nullptr, nullptr, nullptr);
-      cross3(Ba, va, Ep[k]);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) Bp[k][i] = Ba[i];
-      avg_at(mag_neighbor<T, DIM>(a, ic, k, -1), Ba, va, nullptr, nullptr, nullptr, nullptr);
-      cross3(Ba, va, Em[k]);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) Bm[k][i] = Ba[i];
-    }
-    // d(F_i)/d(x_k) = 0.5 (F_i[+] - F_i[-]) / dx
-    auto dF = [&](T (*Fp)[3], T (*Fm)[3], int i, int k) { return T(0.5) * (Fp[k][i] - Fm[k][i]) / dx; };
-    T curlE[3], curlB[3];
-    if (DIM == 2) {
-      curlE[0] = dF(Ep, Em, 2, 1);
-      curlE[1] = -dF(Ep, Em, 2, 0);
-      curlE[2] = dF(Ep, Em, 1, 0) - dF(Ep, Em, 0, 1);
-      curlB[0] = dF(Bp, Bm, 2, 1);
-      curlB[1] = -dF(Bp, Bm, 2, 0);
-      curlB[2] = dF(Bp, Bm, 1, 0) - dF(Bp, Bm, 0, 1);
-    } else {
-      curlE[0] = dF(Ep, Em, 2, 1) - dF(Ep, Em, 1, 2);
-      curlE[1] = dF(Ep, Em, 0, 2) - dF(Ep, Em, 2, 0);
-      curlE[2] = dF(Ep, Em, 1, 0) - dF(Ep, Em, 0, 1);
-      curlB[0] = dF(Bp, Bm, 2, 1) - dF(Bp, Bm, 1, 2);
-      curlB[1] = dF(Bp, Bm, 0, 2) - dF(Bp, Bm, 2, 0);
-      curlB[2] = dF(Bp, Bm, 1, 0) - dF(Bp, Bm, 0, 1);
-    }
-    T phi2[3];
-    cross3(Ba_c, curlB, phi2);
-    const T r = rho[c];
-    T Bn[3], vn[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      Bn[i] = B0c[i] - dt * curlE[i];
-      vn[i] = v0c[i] - dt * (phi2[i] / r);
-    }
-    const T dB = Num<T>::sqrt_(sq(Bc[0] - Bn[0]) + sq(Bc[1] - Bn[1]) + sq(Bc[2] - Bn[2]));
-    const T dv = Num<T>::sqrt_(sq(vc[0] - vn[0]) + sq(vc[1] - vn[1]) + sq(vc[2] - vn[2]));
-    change = nanmax(change, nanmax(dB, dv));
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      dst[i * nc + c] = Bn[i];
-      dst[(3 + i) * nc + c] = vn[i];
-    }
-  }
+       c += (long long)gridDim.x * blockDim.x)
+    mag_direct_cell<T, DIM>(a, src, dst, dt, c, change);
   const double r = block_max<double>((double)change, red);
   if (threadIdx.x == 0) atomic_max_nonneg(slot, r);
 }
@@ -550,134 +576,149 @@ __device__ __forceinline__ void load_iter(const FVArgs<T>& a, const T* src, long
 // the averaged B and of E = B x v is staged in shared memory, so every cell
 // computes its cross product once.  Folds max |B_k - B_{k+1}| and
 // max |v_k - v_{k+1}| into `slot`.
-template <typename T, int DIM>
-__device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, const T* src, T* dst, T dt,
-                                               unsigned long long* slot, double* red, T* smem) {
-  using G = TileGeom<T, DIM>;
+template <typename T, int DIM, int V = 0>
+__device__ __forceinline__ void mag_tile(const FVArgs<T>& a, const int* o, const T* src, T* dst, T dt, T* smem,
+                                         T* change_io) {
+  using G = TileGeom<T, DIM, V>;
   const long long nc = a.ncells;
   const int n = a.n;
   const T dx = T(a.dx);
   const bool midpoint = (a.integrator == 0);
   T* sB = smem;                 // [3][MHALO] averaged B
   T* sE = smem + 3 * G::MHALO;  // [3][MHALO] E = B x v
-  const long long ntiles = fv_num_tiles<DIM>(n, G::T0, G::T1, G::T2);
-  T change = T(0);
+  T change = *change_io;
+  for (int e = threadIdx.x; e < G::MHALO; e += blockDim.x) {
+    const int h2 = e % G::M2, h1 = (e / G::M2) % G::M1, h0 = e / (G::M2 * G::M1);
+    bool fl = false;
+    const int i0 = map_ax<T, DIM>(a, 0, o[0] + h0 - 1, &fl);
+    const int i1 = map_ax<T, DIM>(a, 1, o[1] + h1 - 1, &fl);
+    const int i2 = (DIM >= 3) ? map_ax<T, DIM>(a, 2, o[2] + h2 - 1, &fl) : 0;
+    const long long c = cell_index<DIM>(i0, i1, i2, n);
+    T Bk[3], vk[3], B0[3], v0[3], Ba[3], va[3], E[3];
+    load_iter<T, DIM>(a, src, c, nc, Bk, vk, B0, v0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      Ba[i] = midpoint ? (Bk[i] + B0[i]) / T(2) : Bk[i];
+      va[i] = midpoint ? (vk[i] + v0[i]) / T(2) : vk[i];
+    }
+    cross3(Ba, va, E);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { sB[i * G::MHALO + e] = Ba[i]; sE[i * G::MHALO + e] = E[i]; }
+  }
+  __syncthreads();
+  for (int cl = threadIdx.x; cl < G::CELLS; cl += blockDim.x) {
+    const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
+    const int g0 = o[0] + c0, g1 = o[1] + c1, g2 = o[2] + c2;
+    if (g0 >= n || g1 >= n || (DIM >= 3 && g2 >= n)) continue;
+    const long long c = cell_index<DIM>(g0, g1, g2, n);
+    const int h = ((c0 + 1) * G::M1 + (c1 + 1)) * G::M2 + (DIM >= 3 ? c2 + 1 : 0);
+    const int st[3] = {G::M1 * G::M2, G::M2, 1};
+    // d(F_i)/d(x_k) = 0.5 (F_i[+] - F_i[-]) / dx  (_vector_maths.py:55-100)
+    auto dF = [&](const T* F, int i, int k) {
+      return T(0.5) * (F[i * G::MHALO + h + st[k]] - F[i * G::MHALO + h - st[k]]) / dx;
+    };
+    T curlE[3], curlB[3];
+    if (DIM == 2) {
+      curlE[0] = dF(sE, 2, 1);
+      curlE[1] = -dF(sE, 2, 0);
+      curlE[2] = dF(sE, 1, 0) - dF(sE, 0, 1);
+      curlB[0] = dF(sB, 2, 1);
+      curlB[1] = -dF(sB, 2, 0);
+      curlB[2] = dF(sB, 1, 0) - dF(sB, 0, 1);
+    } else {
+      curlE[0] = dF(sE, 2, 1) - dF(sE, 1, 2);
+      curlE[1] = dF(sE, 0, 2) - dF(sE, 2, 0);
+      curlE[2] = dF(sE, 1, 0) - dF(sE, 0, 1);
+      curlB[0] = dF(sB, 2, 1) - dF(sB, 1, 2);
+      curlB[1] = dF(sB, 0, 2) - dF(sB, 2, 0);
+      curlB[2] = dF(sB, 1, 0) - dF(sB, 0, 1);
+    }
+    T Bk[3], vk[3], B0[3], v0[3], Ba[3];
+    load_iter<T, DIM>(a, src, c, nc, Bk, vk, B0, v0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) Ba[i] = sB[i * G::MHALO + h];
+    T phi2[3];
+    cross3(Ba, curlB, phi2);
+    const T r = a.state[c];
+    T Bn[3], vn[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      Bn[i] = B0[i] - dt * curlE[i];
+      vn[i] = v0[i] - dt * (phi2[i] / r);
+    }
+    const T dB = Num<T>::sqrt_(sq(Bk[0] - Bn[0]) + sq(Bk[1] - Bn[1]) + sq(Bk[2] - Bn[2]));
+    const T dv = Num<T>::sqrt_(sq(vk[0] - vn[0]) + sq(vk[1] - vn[1]) + sq(vk[2] - vn[2]));
+    change = nanmax(change, nanmax(dB, dv));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dst[i * nc + c] = Bn[i];
+      dst[(3 + i) * nc + c] = vn[i];
+    }
+  }
+  __syncthreads();
+  *change_io = change;
+}
 
+template <typename T, int DIM>
+__device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, const T* src, T* dst, T dt,
+                                               unsigned long long* slot, double* red, T* smem) {
+  using G = TileGeom<T, DIM>;
+  const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
+  T change = T(0);
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int o[3];
-    tile_origin<DIM>(tile, n, G::T0, G::T1, G::T2, o);
-    for (int e = threadIdx.x; e < G::MHALO; e += blockDim.x) {
-      const int h2 = e % G::M2, h1 = (e / G::M2) % G::M1, h0 = e / (G::M2 * G::M1);
-      bool fl = false;
-      const int i0 = map_ax<T, DIM>(a, 0, o[0] + h0 - 1, &fl);
-      const int i1 = map_ax<T, DIM>(a, 1, o[1] + h1 - 1, &fl);
-      const int i2 = (DIM >= 3) ? map_ax<T, DIM>(a, 2, o[2] + h2 - 1, &fl) : 0;
-      const long long c = cell_index<DIM>(i0, i1, i2, n);
-      T Bk[3], vk[3], B0[3], v0[3], Ba[3], va[3], E[3];
-      load_iter<T, DIM>(a, src, c, nc, Bk, vk, B0, v0);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        Ba[i] = midpoint ? (Bk[i] + B0[i]) / T(2) : Bk[i];
-        va[i] = midpoint ? (vk[i] + v0[i]) / T(2) : vk[i];
-      }
-      cross3(Ba, va, E);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) { sB[i * G::MHALO + e] = Ba[i]; sE[i * G::MHALO + e] = E[i]; }
-    }
-    __syncthreads();
-    for (int cl = threadIdx.x; cl < G::CELLS; cl += blockDim.x) {
-      const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
-      const int g0 = o[0] + c0, g1 = o[1] + c1, g2 = o[2] + c2;
-      if (g0 >= n || g1 >= n || (DIM >= 3 && g2 >= n)) continue;
-      const long long c = cell_index<DIM>(g0, g1, g2, n);
-      const int h = ((c0 + 1) * G::M1 + (c1 + 1)) * G::M2 + (DIM >= 3 ? c2 + 1 : 0);
-      const int st[3] = {G::M1 * G::M2, G::M2, 1};
-      // d(F_i)/d(x_k) = 0.5 (F_i[+] - F_i[-]) / dx  (_vector_maths.py:55-100)
-      auto dF = [&](const T* F, int i, int k) {
-        return T(0.5) * (F[i * G::MHALO + h + st[k]] - F[i * G::MHALO + h - st[k]]) / dx;
-      };
-      T curlE[3], curlB[3];
-      if (DIM == 2) {
-        curlE[0] = dF(sE, 2, 1);
-        curlE[1] = -dF(sE, 2, 0);
-        curlE[2] = dF(sE, 1, 0) - dF(sE, 0, 1);
-        curlB[0] = dF(sB, 2, 1);
-        curlB[1] = -dF(sB, 2, 0);
-        curlB[2] = dF(sB, 1, 0) - dF(sB, 0, 1);
-      } else {
-        curlE[0] = dF(sE, 2, 1) - dF(sE, 1, 2);
-        curlE[1] = dF(sE, 0, 2) - dF(sE, 2, 0);
-        curlE[2] = dF(sE, 1, 0) - dF(sE, 0, 1);
-        curlB[0] = dF(sB, 2, 1) - dF(sB, 1, 2);
-        curlB[1] = dF(sB, 0, 2) - dF(sB, 2, 0);
-        curlB[2] = dF(sB, 1, 0) - dF(sB, 0, 1);
-      }
-      T Bk[3], vk[3], B0[3], v0[3], Ba[3];
-      load_iter<T, DIM>(a, src, c, nc, Bk, vk, B0, v0);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) Ba[i] = sB[i * G::MHALO + h];
-      T phi2[3];
-      cross3(Ba, curlB, phi2);
-      const T r = a.state[c];
-      T Bn[3], vn[3];
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        Bn[i] = B0[i] - dt * curlE[i];
-        vn[i] = v0[i] - dt * (phi2[i] / r);
-      }
-      const T dB = Num<T>::sqrt_(sq(Bk[0] - Bn[0]) + sq(Bk[1] - Bn[1]) + sq(Bk[2] - Bn[2]));
-      const T dv = Num<T>::sqrt_(sq(vk[0] - vn[0]) + sq(vk[1] - vn[1]) + sq(vk[2] - vn[2]));
-      change = nanmax(change, nanmax(dB, dv));
-#pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        dst[i * nc + c] = Bn[i];
-        dst[(3 + i) * nc + c] = vn[i];
-      }
-    }
-    __syncthreads();
+    tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
+    mag_tile<T, DIM>(a, o, src, dst, dt, smem, &change);
   }
   const double r = block_max<double>((double)change, red);
   if (threadIdx.x == 0) atomic_max_nonneg(slot, r);
 }
 
-// Pressure refresh with gamma = 5/3 and write-back (_magnetic_field_update.py:208-242);
-// folds the maxima of |u_a| + c of the updated gas into `out_slot`.
+// Pressure refresh with gamma = 5/3 and write-back of one cell
+// (_magnetic_field_update.py:208-242); tracks |u_a| + c of the updated gas.
+template <typename T, int DIM>
+__device__ __forceinline__ void mag_finalize_cell(const FVArgs<T>& a, const T* Bv, long long c, bool track,
+                                                  double* m) {
+  const long long nc = a.ncells;
+  const T g53 = T(5.0 / 3.0);
+  const T rho = a.state[c];
+  const T p = a.state[(DIM + 1) * nc + c];
+  T v0[3];
+  v0[0] = a.state[nc + c];
+  v0[1] = a.state[2 * nc + c];
+  v0[2] = (DIM == 3) ? a.state[3 * nc + c] : T(0);
+  T vn[3], Bn[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) { Bn[i] = Bv[i * nc + c]; vn[i] = Bv[(3 + i) * nc + c]; }
+  const T v0abs = Num<T>::sqrt_(v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2]);
+  const T vnabs = Num<T>::sqrt_(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
+  T E = total_energy(rho, v0abs, p, g53);
+  E = E - T(0.5) * rho * (v0abs * v0abs) + T(0.5) * rho * (vnabs * vnabs);
+  const T pn = pressure_from_energy(E, rho, vnabs, g53);
+  T q[DIM + 2];
+  q[0] = rho;
+#pragma unroll
+  for (int i = 0; i < DIM; ++i) {
+    a.state[(1 + i) * nc + c] = vn[i];
+    q[1 + i] = vn[i];
+  }
+  a.state[(DIM + 1) * nc + c] = pn;
+  q[DIM + 1] = pn;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) a.state[(DIM + 2 + i) * nc + c] = Bn[i];
+  if (track) track_maxima<T, DIM>(q, T(a.gamma), m);
+}
+
+// The write-back phase over all cells; folds the maxima of |u_a| + c of the
+// updated gas into `out_slot` when given.
 template <typename T, int DIM>
 __device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* Bv, unsigned long long* out_slot,
                                                 double* red) {
   const long long nc = a.ncells;
-  const T g53 = T(5.0 / 3.0);
-  const T gamma = T(a.gamma);
   double m[3] = {0.0, 0.0, 0.0};
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (long long)gridDim.x * blockDim.x) {
-    const T rho = a.state[c];
-    const T p = a.state[(DIM + 1) * nc + c];
-    T v0[3];
-    v0[0] = a.state[nc + c];
-    v0[1] = a.state[2 * nc + c];
-    v0[2] = (DIM == 3) ? a.state[3 * nc + c] : T(0);
-    T vn[3], Bn[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) { Bn[i] = Bv[i * nc + c]; vn[i] = Bv[(3 + i) * nc + c]; }
-    const T v0abs = Num<T>::sqrt_(v0[0] * v0[0] + v0[1] * v0[1] + v0[2] * v0[2]);
-    const T vnabs = Num<T>::sqrt_(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
-    T E = total_energy(rho, v0abs, p, g53);
-    E = E - T(0.5) * rho * (v0abs * v0abs) + T(0.5) * rho * (vnabs * vnabs);
-    const T pn = pressure_from_energy(E, rho, vnabs, g53);
-    T q[DIM + 2];
-    q[0] = rho;
-#pragma unroll
-    for (int i = 0; i < DIM; ++i) {
-      a.state[(1 + i) * nc + c] = vn[i];
-      q[1 + i] = vn[i];
-    }
-    a.state[(DIM + 1) * nc + c] = pn;
-    q[DIM + 1] = pn;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) a.state[(DIM + 2 + i) * nc + c] = Bn[i];
-    if (out_slot) track_maxima<T, DIM>(q, gamma, m);
-  }
+       c += (long long)gridDim.x * blockDim.x)
+    mag_finalize_cell<T, DIM>(a, Bv, c, out_slot != nullptr, m);
   if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
 

@@ -210,6 +210,47 @@ int amx_status(amx_plan* plan, int32_t* status_host, int32_t clear, void* stream
 int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_params* prm, int64_t max_steps,
                        amx_run_info* info, void* stream);
 
+/* ---- batched ensemble ----------------------------------------------------- */
+
+/* No counterpart in the reference, which integrates one simulation per
+ * time_integration call (astronomix/time_stepping/time_integration.py:61-236);
+ * an ensemble there is a Python loop over that call.  A batch advances up to
+ * 256 independent 2D FV runs of uneven grid sizes with one persistent
+ * cooperative launch.  Every run follows amx_run exactly (bit-identical
+ * results) with its own dt, time, end time and fixed-point iteration count.
+ * The runs share the template configuration `tmpl` (dtype, MHD, HLL / HLLC /
+ * HLLC-LM, limiter, boundaries, magnetic integrator; adaptive dt only) and
+ * the parameters other than t_end; run r has num_cells[r]^2 cells on a box of
+ * side box_size[r] (tmpl->num_cells and tmpl->grid_spacing are ignored). */
+typedef struct amx_batch amx_batch;
+int amx_batch_create(const amx_config* tmpl, int32_t num_runs, const int32_t* num_cells, const double* box_size,
+                     amx_batch** out);
+int amx_batch_destroy(amx_batch* batch);
+int amx_batch_workspace_bytes(const amx_batch* batch, size_t* bytes);
+/* Time, step counters and status of every run back to zero (stream-ordered). */
+int amx_batch_reset(amx_batch* batch, void* stream);
+/* Advances every run r (states[r]: device state of run r, in place) until
+ * t_r >= t_end[r], or for at most `max_steps` lock-step steps, in one
+ * cooperative launch.  With use_graph != 0 the launch is captured once into
+ * a CUDA graph and replayed while the arguments and the tiling stay the same.
+ * Does not synchronise. */
+int amx_batch_run(amx_batch* batch, void* const* states, const amx_params* prm, const double* t_end,
+                  int64_t max_steps, int32_t use_graph, void* stream);
+/* Per-run progress (infos[num_runs]) and the lock-step steps taken so far
+ * (synchronises). */
+int amx_batch_info(amx_batch* batch, amx_run_info* infos, int64_t* lock_steps, void* stream);
+/* Autotuner: times `steps` lock-step steps of copies of the states under
+ * every compiled tile shape and resident-block count and keeps the fastest
+ * (the states and counters are left as they were; *best_ms, if non-null,
+ * gets the winning time).  Synchronises. */
+int amx_batch_tune(amx_batch* batch, void* const* states, const amx_params* prm, const double* t_end,
+                   int32_t steps, double* best_ms, void* stream);
+/* Current tiling: shape variant, resident blocks per SM, tile extent. */
+int amx_batch_tiling(const amx_batch* batch, int32_t* variant, int32_t* blocks_per_sm, int32_t* tile0,
+                     int32_t* tile1);
+/* Forces a tiling (blocks_per_sm <= 0 picks the default). */
+int amx_batch_set_tiling(amx_batch* batch, int32_t variant, int32_t blocks_per_sm);
+
 /* Library version string. */
 const char* amx_version(void);
 
