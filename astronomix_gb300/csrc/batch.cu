@@ -185,9 +185,10 @@ int launch_graph(amx_batch* b, amx::BatchArgs<T>& a, cudaStream_t s) {
 }
 
 // Points the device table at `states` with end times `t_end`; uploads only
-// when something changed (synchronous copy: the table is small and changes
+// when something changed, after the work queued on `s` (which may read the
+// table) has finished (synchronous copy: the table is small and changes
 // rarely).
-int set_table(amx_batch* b, void* const* states, const double* t_end) {
+int set_table(amx_batch* b, void* const* states, const double* t_end, cudaStream_t s) {
   bool changed = false;
   for (int r = 0; r < b->num_runs; ++r) {
     if (b->desc[r].state != states[r] || b->desc[r].t_end != t_end[r]) {
@@ -197,6 +198,7 @@ int set_table(amx_batch* b, void* const* states, const double* t_end) {
     }
   }
   if (!changed) return AMX_OK;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return AMX_ERR_CUDA;
   return cuda_ok(cudaMemcpy(b->d_desc, b->desc.data(), sizeof(BatchRunDesc) * b->num_runs,
                             cudaMemcpyHostToDevice));
 }
@@ -330,7 +332,7 @@ int amx_batch_run(amx_batch* b, void* const* states, const amx_params* prm, cons
   if (!b || !states || !prm || !t_end || max_steps < 0) return AMX_ERR_INVALID_ARG;
   for (int r = 0; r < b->num_runs; ++r)
     if (!states[r]) return AMX_ERR_INVALID_ARG;
-  int rc = set_table(b, states, t_end);
+  int rc = set_table(b, states, t_end, static_cast<cudaStream_t>(stream));
   if (rc) return rc;
   if (max_steps == 0) return AMX_OK;
   return run_once(b, prm, max_steps, use_graph != 0, static_cast<cudaStream_t>(stream));
@@ -381,7 +383,9 @@ int amx_batch_tune(amx_batch* b, void* const* states, const amx_params* prm, con
   const int nvars = b->cfg.num_vars;
   // trial runs work on copies of the states and restore the run control
   std::vector<BatchRunCtl> saved(R);
+  BatchControl saved_ctl{};
   int rc = cuda_ok(cudaMemcpyAsync(saved.data(), b->d_rctl, sizeof(BatchRunCtl) * R, cudaMemcpyDeviceToHost, s));
+  rc |= cuda_ok(cudaMemcpyAsync(&saved_ctl, b->d_ctl, sizeof(saved_ctl), cudaMemcpyDeviceToHost, s));
   rc |= cuda_ok(cudaStreamSynchronize(s));
   if (rc) return rc;
   std::vector<size_t> bytes(R), offs(R);
@@ -410,7 +414,7 @@ int amx_batch_tune(amx_batch* b, void* const* states, const amx_params* prm, con
     r2 |= cuda_ok(cudaStreamSynchronize(s));
     return r2;
   };
-  rc = set_table(b, trial.data(), t_end);
+  rc = set_table(b, trial.data(), t_end, s);
   for (int v = 0; v < amx::kBatchVariants && !rc; ++v) {
     BatchKernelInfo k{};
     if (!lookup(b, v, &k)) continue;
@@ -440,9 +444,9 @@ int amx_batch_tune(amx_batch* b, void* const* states, const amx_params* prm, con
   }
   // back to the caller's states and counters, with the fastest tiling
   int rc2 = cuda_ok(cudaMemcpyAsync(b->d_rctl, saved.data(), sizeof(BatchRunCtl) * R, cudaMemcpyHostToDevice, s));
-  rc2 |= cuda_ok(cudaMemsetAsync(&b->d_ctl->status, 0, sizeof(int), s));
+  rc2 |= cuda_ok(cudaMemcpyAsync(b->d_ctl, &saved_ctl, sizeof(saved_ctl), cudaMemcpyHostToDevice, s));
   rc2 |= cuda_ok(cudaStreamSynchronize(s));
-  rc2 |= set_table(b, states, t_end);
+  rc2 |= set_table(b, states, t_end, s);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(scratch);

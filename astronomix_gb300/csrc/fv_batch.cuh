@@ -205,8 +205,8 @@ fv_batch_kernel(BatchArgs<T> b) {
       const T h = T(s_dt[r]) / div;  // the single-run kernel's dtT / 2 (MHD) or dtT
       const T* in = from_state ? a.state : a.p1;
       T* out = from_state ? a.p1 : a.state;
-      hydro_tile<T, DIM, RS, V>(a, o, in, out, p0_is_state ? a.state : nullptr, h, RS == RS_LF ? alpha : nullptr,
-                                smem, m, track);
+      FVItems<T, DIM, RS, V>::hydro(a, o, in, out, p0_is_state ? a.state : nullptr, h,
+                                    RS == RS_LF ? alpha : nullptr, smem, m, track);
     }
     if (track && cur >= 0) batch_fold<DIM>(m, rc[cur].red[rp % 3], red);
     ++rp;
@@ -250,7 +250,7 @@ fv_batch_kernel(BatchArgs<T> b) {
       const long long c0 = (long long)(g - s_pref[r]) * kBatchChunk;
       const long long c1 = min(nc, c0 + kBatchChunk);
       const T h = T(s_dt[r]);
-      for (long long c = c0 + threadIdx.x; c < c1; c += blockDim.x) mag_direct_cell<T, DIM>(a, ms, dst, h, c, change);
+      MagItems<T, DIM>::direct(a, ms, dst, h, c0 + threadIdx.x, c1, blockDim.x, &change);
     }
     if (cur >= 0) {
       const double v = block_max<double>((double)change, red);
@@ -315,7 +315,7 @@ fv_batch_kernel(BatchArgs<T> b) {
       const T* Bv = (s_flag[r] & 4) ? a.mag1 : a.mag0;
       const long long c0 = (long long)(g - s_pref[r]) * kBatchChunk;
       const long long c1 = min(a.ncells, c0 + kBatchChunk);
-      for (long long c = c0 + threadIdx.x; c < c1; c += blockDim.x) mag_finalize_cell<T, DIM>(a, Bv, c, track, m);
+      MagItems<T, DIM>::finalize(a, Bv, c0 + threadIdx.x, c1, blockDim.x, track, m);
     }
     if (track && cur >= 0) batch_fold<DIM>(m, rc[cur].red[rp % 3], red);
     ++rp;

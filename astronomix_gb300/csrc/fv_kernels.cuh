@@ -84,6 +84,10 @@ struct FVArgs {
   double t_pause;    // full-step mode stops before a step that starts at t >= t_pause
 };
 
+// per-item entry points, defined below
+template <typename T, int DIM, int RS, int V> struct FVItems;
+template <typename T, int DIM> struct MagItems;
+
 // ---------------------------------------------------------------- tiles
 
 template <typename T, int DIM> struct Tile;
@@ -175,15 +179,27 @@ __device__ __forceinline__ long long cell_index(int i0, int i1, int i2, int n) {
   return ((long long)i0 * n + i1) * n + i2;
 }
 
-// maps a logical (possibly out-of-domain) index onto the stored grid
-template <typename T, int DIM>
-__device__ __forceinline__ int map_ax(const FVArgs<T>& a, int k, int g, bool* flip) {
-  const int n = a.n;
-  if (g < -2) g = -2;
-  if (g > n + 1) g = n + 1;
-  if (a.periodic_roll) return wrap(g, n);
-  return map_index(g, n, a.bc[k], DIM == 1, flip);
-}
+// Maps a logical (possibly out-of-domain, clamped to [-2, n+1]) index onto
+// the stored grid.  The boundary settings are copied into registers: FVArgs
+// is read through a reference, so its fields would be reloaded after every
+// store.
+template <int DIM>
+struct AxisMap {
+  int n;
+  bool roll;
+  AxisBC bc[3];
+  template <typename T>
+  __device__ __forceinline__ explicit AxisMap(const FVArgs<T>& a) : n(a.n), roll(a.periodic_roll != 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) bc[k] = a.bc[k];
+  }
+  __device__ __forceinline__ int operator()(int k, int g, bool* flip) const {
+    if (g < -2) g = -2;
+    if (g > n + 1) g = n + 1;
+    if (roll) return wrap(g, n);
+    return map_index(g, n, bc[k], DIM == 1, flip);
+  }
+};
 
 // ------------------------------------------------------------ reductions
 
@@ -211,11 +227,12 @@ __device__ __noinline__ void phase_cfl(const FVArgs<T>& a, unsigned long long* s
   const T gamma = T(a.gamma);
   double m[3] = {0.0, 0.0, 0.0};
   const long long nc = a.ncells;
+  const T* st = a.state;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
        c += (long long)gridDim.x * blockDim.x) {
     T q[DIM + 2];
 #pragma unroll
-    for (int v = 0; v < DIM + 2; ++v) q[v] = a.state[v * nc + c];
+    for (int v = 0; v < DIM + 2; ++v) q[v] = st[v * nc + c];
     track_maxima<T, DIM>(q, gamma, m);
   }
   fold_maxima<DIM>(m, slot, red);
@@ -242,6 +259,9 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
   const T gamma = T(a.gamma);
   const T dxT = T(a.dx);
   const T inv_dx = T(1.0 / a.dx);
+  const int limiter = a.limiter;
+  const bool lm = a.lm != 0;
+  const AxisMap<DIM> amap(a);
   T* sP = smem;                        // [NV][HALO]
   T* sF = smem + NV * G::HALO;         // [NV][FMAX]
   T* sD = sF + NV * G::FMAX;           // [NV][SMAX] slopes (already * dx / 2)
@@ -252,9 +272,9 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
     const int h1 = (e / G::H2) % G::H1;
     const int h0 = e / (G::H2 * G::H1);
     bool f0 = false, f1 = false, f2 = false;
-    const int i0 = map_ax<T, DIM>(a, 0, o[0] + h0 - 2, &f0);
-    const int i1 = (DIM >= 2) ? map_ax<T, DIM>(a, 1, o[1] + h1 - 2, &f1) : 0;
-    const int i2 = (DIM >= 3) ? map_ax<T, DIM>(a, 2, o[2] + h2 - 2, &f2) : 0;
+    const int i0 = amap(0, o[0] + h0 - 2, &f0);
+    const int i1 = (DIM >= 2) ? amap(1, o[1] + h1 - 2, &f1) : 0;
+    const int i2 = (DIM >= 3) ? amap(2, o[2] + h2 - 2, &f2) : 0;
     const long long c = cell_index<DIM>(i0, i1, i2, n);
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
@@ -302,7 +322,7 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
         for (int v = 0; v < NV; ++v) {
           const T* s = sP + v * G::HALO + h;
           const T qm = s[-stride], q0 = s[0], qp = s[stride];
-          sDk[v * sdim + e] = limited((q0 - qm) / dxT, (qp - q0) / dxT, a.limiter, dxT) * dxT / T(2);
+          sDk[v * sdim + e] = limited((q0 - qm) / dxT, (qp - q0) / dxT, limiter, dxT) * dxT / T(2);
         }
       }
     }
@@ -335,14 +355,14 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
             qR[v] = s[0] - d[0];
           } else {
             const T qm2 = s[-2 * stride], qm1 = s[-stride], q0 = s[0], qp1 = s[stride];
-            const T gm1 = limited((qm1 - qm2) / dxT, (q0 - qm1) / dxT, a.limiter, dxT);
-            const T g0 = limited((q0 - qm1) / dxT, (qp1 - q0) / dxT, a.limiter, dxT);
+            const T gm1 = limited((qm1 - qm2) / dxT, (q0 - qm1) / dxT, limiter, dxT);
+            const T g0 = limited((q0 - qm1) / dxT, (qp1 - q0) / dxT, limiter, dxT);
             qL[v] = qm1 + gm1 * dxT / T(2);
             qR[v] = q0 - g0 * dxT / T(2);
           }
         }
         T F[NV];
-        riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), a.lm != 0, F);
+        riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), lm, F);
 #pragma unroll
         for (int v = 0; v < NV; ++v) sFk[v * fdim + f] = F[v];
       }
@@ -408,7 +428,7 @@ __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __re
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int o[3];
     tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
-    hydro_tile<T, DIM, RS>(a, o, Pin, Pout, P0, dt, alpha, smem, m, out_slot != nullptr);
+    FVItems<T, DIM, RS, 0>::hydro(a, o, Pin, Pout, P0, dt, alpha, smem, m, out_slot != nullptr);
   }
   if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
@@ -442,27 +462,37 @@ __device__ __forceinline__ void load_Bv(const MagSrc<T, DIM>& s, long long c, lo
   v[2] = (DIM == 2 && s.from_gas) ? T(0) : s.v[2 * nc + c];
 }
 
+// The fields of FVArgs the point-wise magnetic work reads, copied into
+// registers once per range of cells (read through the FVArgs reference, they
+// would be reloaded after every global store, which may alias them).
 template <typename T, int DIM>
-__device__ __forceinline__ long long mag_neighbor(const FVArgs<T>& a, const int* ic, int k, int off) {
-  int j[3] = {ic[0], ic[1], ic[2]};
-  bool flip = false;
-  j[k] = map_ax<T, DIM>(a, k, ic[k] + off, &flip);
-  return cell_index<DIM>(j[0], j[1], j[2], a.n);
-}
+struct MagCtx {
+  T* state;
+  long long nc;
+  int n;
+  T dx;
+  bool midpoint;
+  AxisMap<DIM> amap;
+  __device__ __forceinline__ explicit MagCtx(const FVArgs<T>& a)
+      : state(a.state), nc(a.ncells), n(a.n), dx(T(a.dx)), midpoint(a.integrator == 0), amap(a) {}
+  // the cell `off` cells away along axis k, boundary-mapped
+  __device__ __forceinline__ long long neighbor(const int* ic, int k, int off) const {
+    int j[3] = {ic[0], ic[1], ic[2]};
+    bool flip = false;
+    j[k] = amap(k, ic[k] + off, &flip);
+    return cell_index<DIM>(j[0], j[1], j[2], n);
+  }
+};
 
-// One evaluation of the fixed-point map without shared memory: every cell
-// gathers the averaged fields of its 2*DIM neighbours itself (L1 serves the
-// reuse).  Used when the state is L2-resident (2D), where the tiled variant
-// below loses more to tile imbalance and barriers than it saves in loads.
 template <typename T, int DIM>
-__device__ __forceinline__ void mag_direct_cell(const FVArgs<T>& a, const MagSrc<T, DIM>& src, T* dst, T dt,
+__device__ __forceinline__ void mag_direct_cell(const MagCtx<T, DIM>& x, const MagSrc<T, DIM>& src, T* dst, T dt,
                                                 long long c, T& change) {
-  const long long nc = a.ncells;
-  const int n = a.n;
-  const T dx = T(a.dx);
-  const MagSrc<T, DIM> s0{a.state + (DIM + 2) * nc, a.state + nc, true};  // B0, v0
-  const T* rho = a.state;
-  const bool midpoint = (a.integrator == 0);
+  const long long nc = x.nc;
+  const int n = x.n;
+  const T dx = x.dx;
+  const MagSrc<T, DIM> s0{x.state + (DIM + 2) * nc, x.state + nc, true};  // B0, v0
+  const T* rho = x.state;
+  const bool midpoint = x.midpoint;
   int ic[3];
   if (DIM == 2) { ic[0] = (int)(c / n); ic[1] = (int)(c % n); ic[2] = 0; }
   else { ic[2] = (int)(c % n); ic[1] = (int)((c / n) % n); ic[0] = (int)(c / ((long long)n * n)); }
@@ -486,11 +516,11 @@ __device__ __forceinline__ void mag_direct_cell(const FVArgs<T>& a, const MagSrc
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
     T Ba[3], va[3];
-    avg_at(mag_neighbor<T, DIM>(a, ic, k, +1), Ba, va, nullptr, nullptr, nullptr, nullptr);
+    avg_at(x.neighbor(ic, k, +1), Ba, va, nullptr, nullptr, nullptr, nullptr);
     cross3(Ba, va, Ep[k]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) Bp[k][i] = Ba[i];
-    avg_at(mag_neighbor<T, DIM>(a, ic, k, -1), Ba, va, nullptr, nullptr, nullptr, nullptr);
+    avg_at(x.neighbor(ic, k, -1), Ba, va, nullptr, nullptr, nullptr, nullptr);
     cross3(Ba, va, Em[k]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) Bm[k][i] = Ba[i];
@@ -541,9 +571,8 @@ __device__ __noinline__ void phase_mag_iterate_direct(const FVArgs<T>& a, MagSrc
                                   unsigned long long* slot, double* red) {
   const long long nc = a.ncells;
   T change = T(0);
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (long long)gridDim.x * blockDim.x)
-    mag_direct_cell<T, DIM>(a, src, dst, dt, c, change);
+  MagItems<T, DIM>::direct(a, src, dst, dt, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
+                           (long long)gridDim.x * blockDim.x, &change);
   const double r = block_max<double>((double)change, red);
   if (threadIdx.x == 0) atomic_max_nonneg(slot, r);
 }
@@ -552,9 +581,8 @@ __device__ __noinline__ void phase_mag_iterate_direct(const FVArgs<T>& a, MagSrc
 // first evaluation, which starts from B0 and v0 (the state's B rows and gas
 // velocity, vz = 0 in 2D as in _magnetic_field_update.py:60-70).
 template <typename T, int DIM>
-__device__ __forceinline__ void load_iter(const FVArgs<T>& a, const T* src, long long c, long long nc, T* Bk,
+__device__ __forceinline__ void load_iter(const T* st, const T* src, long long c, long long nc, T* Bk,
                                           T* vk, T* B0, T* v0) {
-  const T* st = a.state;
   B0[0] = st[(DIM + 2) * nc + c];
   B0[1] = st[(DIM + 3) * nc + c];
   B0[2] = st[(DIM + 4) * nc + c];
@@ -584,18 +612,20 @@ __device__ __forceinline__ void mag_tile(const FVArgs<T>& a, const int* o, const
   const int n = a.n;
   const T dx = T(a.dx);
   const bool midpoint = (a.integrator == 0);
+  const T* state = a.state;
+  const AxisMap<DIM> amap(a);
   T* sB = smem;                 // [3][MHALO] averaged B
   T* sE = smem + 3 * G::MHALO;  // [3][MHALO] E = B x v
   T change = *change_io;
   for (int e = threadIdx.x; e < G::MHALO; e += blockDim.x) {
     const int h2 = e % G::M2, h1 = (e / G::M2) % G::M1, h0 = e / (G::M2 * G::M1);
     bool fl = false;
-    const int i0 = map_ax<T, DIM>(a, 0, o[0] + h0 - 1, &fl);
-    const int i1 = map_ax<T, DIM>(a, 1, o[1] + h1 - 1, &fl);
-    const int i2 = (DIM >= 3) ? map_ax<T, DIM>(a, 2, o[2] + h2 - 1, &fl) : 0;
+    const int i0 = amap(0, o[0] + h0 - 1, &fl);
+    const int i1 = amap(1, o[1] + h1 - 1, &fl);
+    const int i2 = (DIM >= 3) ? amap(2, o[2] + h2 - 1, &fl) : 0;
     const long long c = cell_index<DIM>(i0, i1, i2, n);
     T Bk[3], vk[3], B0[3], v0[3], Ba[3], va[3], E[3];
-    load_iter<T, DIM>(a, src, c, nc, Bk, vk, B0, v0);
+    load_iter<T, DIM>(state, src, c, nc, Bk, vk, B0, v0);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       Ba[i] = midpoint ? (Bk[i] + B0[i]) / T(2) : Bk[i];
@@ -634,12 +664,12 @@ __device__ __forceinline__ void mag_tile(const FVArgs<T>& a, const int* o, const
       curlB[2] = dF(sB, 1, 0) - dF(sB, 0, 1);
     }
     T Bk[3], vk[3], B0[3], v0[3], Ba[3];
-    load_iter<T, DIM>(a, src, c, nc, Bk, vk, B0, v0);
+    load_iter<T, DIM>(state, src, c, nc, Bk, vk, B0, v0);
 #pragma unroll
     for (int i = 0; i < 3; ++i) Ba[i] = sB[i * G::MHALO + h];
     T phi2[3];
     cross3(Ba, curlB, phi2);
-    const T r = a.state[c];
+    const T r = state[c];
     T Bn[3], vn[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -677,16 +707,15 @@ __device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, const T* src,
 // Pressure refresh with gamma = 5/3 and write-back of one cell
 // (_magnetic_field_update.py:208-242); tracks |u_a| + c of the updated gas.
 template <typename T, int DIM>
-__device__ __forceinline__ void mag_finalize_cell(const FVArgs<T>& a, const T* Bv, long long c, bool track,
-                                                  double* m) {
-  const long long nc = a.ncells;
+__device__ __forceinline__ void mag_finalize_cell(T* state, long long nc, T gamma, const T* Bv, long long c,
+                                                  bool track, double* m) {
   const T g53 = T(5.0 / 3.0);
-  const T rho = a.state[c];
-  const T p = a.state[(DIM + 1) * nc + c];
+  const T rho = state[c];
+  const T p = state[(DIM + 1) * nc + c];
   T v0[3];
-  v0[0] = a.state[nc + c];
-  v0[1] = a.state[2 * nc + c];
-  v0[2] = (DIM == 3) ? a.state[3 * nc + c] : T(0);
+  v0[0] = state[nc + c];
+  v0[1] = state[2 * nc + c];
+  v0[2] = (DIM == 3) ? state[3 * nc + c] : T(0);
   T vn[3], Bn[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) { Bn[i] = Bv[i * nc + c]; vn[i] = Bv[(3 + i) * nc + c]; }
@@ -699,15 +728,76 @@ __device__ __forceinline__ void mag_finalize_cell(const FVArgs<T>& a, const T* B
   q[0] = rho;
 #pragma unroll
   for (int i = 0; i < DIM; ++i) {
-    a.state[(1 + i) * nc + c] = vn[i];
+    state[(1 + i) * nc + c] = vn[i];
     q[1 + i] = vn[i];
   }
-  a.state[(DIM + 1) * nc + c] = pn;
+  state[(DIM + 1) * nc + c] = pn;
   q[DIM + 1] = pn;
 #pragma unroll
-  for (int i = 0; i < 3; ++i) a.state[(DIM + 2 + i) * nc + c] = Bn[i];
-  if (track) track_maxima<T, DIM>(q, T(a.gamma), m);
+  for (int i = 0; i < 3; ++i) state[(DIM + 2 + i) * nc + c] = Bn[i];
+  if (track) track_maxima<T, DIM>(q, gamma, m);
 }
+
+// ------------------------------------------------------------ per-item entry points
+
+// The work items of the FV step as the single-run and the batched kernels
+// call them: one hydro tile, and a strided range of cells of the fixed-point
+// map or of the write-back.  In FP64 they are separate (not inlined)
+// functions, so both kernels execute the same compiled arithmetic: IEEE
+// division leaves branches in the code around which the compiler may fuse
+// multiply-adds differently in different callers.  In FP32 (approximate
+// division, straight-line code) inlining already gives identical results.
+template <typename T, int DIM, int RS, int V>
+struct FVItems {
+  static __device__ __forceinline__ void hydro(const FVArgs<T>& a, const int* o, const T* Pin, T* Pout,
+                                               const T* P0, T dt, const T* alpha, T* smem, double* m, bool track) {
+    hydro_tile<T, DIM, RS, V>(a, o, Pin, Pout, P0, dt, alpha, smem, m, track);
+  }
+};
+template <int DIM, int RS, int V>
+struct FVItems<double, DIM, RS, V> {
+  static __device__ __noinline__ void hydro(const FVArgs<double>& a, const int* o, const double* Pin, double* Pout,
+                                            const double* P0, double dt, const double* alpha, double* smem,
+                                            double* m, bool track) {
+    hydro_tile<double, DIM, RS, V>(a, o, Pin, Pout, P0, dt, alpha, smem, m, track);
+  }
+};
+
+template <typename T, int DIM>
+struct MagItems {
+  static __device__ __forceinline__ void direct(const FVArgs<T>& a, const MagSrc<T, DIM>& src, T* dst, T dt,
+                                                long long c, long long end, long long step, T* change) {
+    const MagCtx<T, DIM> x(a);
+    T ch = *change;
+    for (; c < end; c += step) mag_direct_cell<T, DIM>(x, src, dst, dt, c, ch);
+    *change = ch;
+  }
+  static __device__ __forceinline__ void finalize(const FVArgs<T>& a, const T* Bv, long long c, long long end,
+                                                  long long step, bool track, double* m) {
+    T* state = a.state;
+    const long long nc = a.ncells;
+    const T gamma = T(a.gamma);
+    for (; c < end; c += step) mag_finalize_cell<T, DIM>(state, nc, gamma, Bv, c, track, m);
+  }
+};
+template <int DIM>
+struct MagItems<double, DIM> {
+  static __device__ __noinline__ void direct(const FVArgs<double>& a, const MagSrc<double, DIM>& src, double* dst,
+                                             double dt, long long c, long long end, long long step,
+                                             double* change) {
+    const MagCtx<double, DIM> x(a);
+    double ch = *change;
+    for (; c < end; c += step) mag_direct_cell<double, DIM>(x, src, dst, dt, c, ch);
+    *change = ch;
+  }
+  static __device__ __noinline__ void finalize(const FVArgs<double>& a, const double* Bv, long long c,
+                                               long long end, long long step, bool track, double* m) {
+    double* state = a.state;
+    const long long nc = a.ncells;
+    const double gamma = a.gamma;
+    for (; c < end; c += step) mag_finalize_cell<double, DIM>(state, nc, gamma, Bv, c, track, m);
+  }
+};
 
 // The write-back phase over all cells; folds the maxima of |u_a| + c of the
 // updated gas into `out_slot` when given.
@@ -716,9 +806,8 @@ __device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* Bv,
                                                 double* red) {
   const long long nc = a.ncells;
   double m[3] = {0.0, 0.0, 0.0};
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (long long)gridDim.x * blockDim.x)
-    mag_finalize_cell<T, DIM>(a, Bv, c, out_slot != nullptr, m);
+  MagItems<T, DIM>::finalize(a, Bv, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
+                             (long long)gridDim.x * blockDim.x, out_slot != nullptr, m);
   if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
 
