@@ -127,6 +127,13 @@ SIGNATURES = {
     "amx_batch_tiling": (_I32, [_P, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I32),
                                 ctypes.POINTER(_I32)]),
     "amx_batch_set_tiling": (_I32, [_P, _I32, _I32]),
+    "amx_adjoint_create": (_I32, [ctypes.POINTER(amx_config), _I32, _I64, ctypes.POINTER(_P)]),
+    "amx_adjoint_destroy": (_I32, [_P]),
+    "amx_adjoint_forward": (_I32, [_P, _P, ctypes.POINTER(amx_params), ctypes.POINTER(amx_run_info), _P]),
+    "amx_adjoint_backward": (_I32, [_P, _P, _P, _P]),
+    "amx_adjoint_replay": (_I32, [_P, _P, _P]),
+    "amx_adjoint_schedule": (_I32, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I32), _I64, ctypes.POINTER(_I64)]),
+    "amx_adjoint_memory": (_I32, [_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     "amx_version": (ctypes.c_char_p, []),
 }
 
@@ -313,3 +320,51 @@ class Batch:
 
     def set_tiling(self, variant, blocks_per_sm=0):
         check(self._L.amx_batch_set_tiling(self.handle, int(variant), int(blocks_per_sm)), "amx_batch_set_tiling")
+
+
+class Adjoint:
+    """Owns an ``amx_adjoint``: checkpoints, schedule and tape of the
+    reverse-mode gradient of one FV configuration."""
+
+    def __init__(self, cfg: amx_config, checkpoint_every=20, max_steps=1 << 20):
+        self._L = lib()
+        h = ctypes.c_void_p()
+        check(self._L.amx_adjoint_create(ctypes.byref(cfg), int(checkpoint_every), int(max_steps), ctypes.byref(h)),
+              "amx_adjoint_create")
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self._L.amx_adjoint_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def forward(self, state_ptr, prm: amx_params, stream=0) -> amx_run_info:
+        info = amx_run_info()
+        check(self._L.amx_adjoint_forward(self.handle, _P(state_ptr), ctypes.byref(prm), ctypes.byref(info),
+                                          _P(stream)), "amx_adjoint_forward")
+        return info
+
+    def backward(self, grad_final_ptr, grad_initial_ptr, stream=0):
+        check(self._L.amx_adjoint_backward(self.handle, _P(grad_final_ptr), _P(grad_initial_ptr), _P(stream)),
+              "amx_adjoint_backward")
+
+    def replay(self, state_ptr, stream=0):
+        check(self._L.amx_adjoint_replay(self.handle, _P(state_ptr), _P(stream)), "amx_adjoint_replay")
+
+    def schedule(self):
+        steps = ctypes.c_int64()
+        check(self._L.amx_adjoint_schedule(self.handle, None, None, 0, ctypes.byref(steps)), "amx_adjoint_schedule")
+        n = steps.value
+        dts = (ctypes.c_double * max(n, 1))()
+        its = (ctypes.c_int32 * max(n, 1))()
+        check(self._L.amx_adjoint_schedule(self.handle, dts, its, n, None), "amx_adjoint_schedule")
+        return list(dts)[:n], list(its)[:n]
+
+    def memory(self):
+        a, b = ctypes.c_size_t(), ctypes.c_size_t()
+        check(self._L.amx_adjoint_memory(self.handle, ctypes.byref(a), ctypes.byref(b)), "amx_adjoint_memory")
+        return {"checkpoint_bytes": a.value, "tape_bytes": b.value}

@@ -1,0 +1,770 @@
+// Discrete adjoint of the finite-volume MHD step (reverse mode, by hand).
+//
+// The forward step (fv_kernels.cuh) is
+//
+//   S1 = L(S0, h)                 stage 1, h = dt/2 (dt without MHD)
+//   S2 = C(S0, L(S1, h))          stage 2 with the RK2 combination
+//   Z0 = G(B0, v0), Z(j+1) = G(Zj)    fixed-point evaluations of the magnetic map
+//   S3 = W(S2, Zk)                write-back (pressure refresh)
+//   S4 = L(S3, h), S5 = C(S3, L(S4, h))
+//
+// with L(P, h) = prim(cons(P) + h/dx sum_axes (F[i-1/2] - F[i+1/2])),
+// C(P0, P) = prim((cons(P0) + cons(P)) / 2) (evolve_state.py:339-488) and G
+// the implicit-midpoint map of _magnetic_field_update.py:82-165.  Its
+// vector-Jacobian products, derived by hand, run as stream-ordered kernels
+// over a tape of S0..S4 and the iterates Zj that a forward replay records
+// with the forward's own dt and iteration count (dt is not differentiated:
+// time_integration.py:632-661 wraps it in stop_gradient; the fixed point is
+// differentiated through the iterations it took, like reverse mode through
+// the reference's while loop).
+//
+// Derivative conventions follow JAX (and torch.autograd): d|x| = sign(x) dx
+// with sign(0) = 0, d sign = 0, and min/max split the cotangent equally on
+// ties.  Two compositions that are the identity in exact arithmetic are
+// differentiated as the identity: cons(prim(U)) inside the RK2 combination
+// and the gamma = 5/3 pressure refresh (p_new = p when the kinetic energy is
+// removed and added back; _magnetic_field_update.py:208-222).  Where the
+// reference evaluates |v| as a square root of zero (the refresh at v = 0),
+// reverse mode through it gives NaN; the identity gives the finite limit.
+//
+// Scope: periodic boundaries, MINMOD limiter, HLL fluxes, implicit midpoint
+// or implicit Euler magnetic integrator, 2D and 3D.
+#pragma once
+
+#include "fv_kernels.cuh"
+
+namespace amx {
+namespace adj {
+
+constexpr int kThreads = 256;
+
+// ------------------------------------------------------------ scalar rules
+
+// d jmax(x, y): weight of x (ties split equally)
+template <typename T> __device__ __forceinline__ T wmax(T x, T y) {
+  return x > y ? T(1) : (x == y ? T(0.5) : T(0));
+}
+template <typename T> __device__ __forceinline__ T wmin(T x, T y) {
+  return x < y ? T(1) : (x == y ? T(0.5) : T(0));
+}
+
+// partial derivatives of minmod(a, b) = (sign a + sign b)/2 * min(|a|, |b|)
+template <typename T>
+__device__ __forceinline__ void minmod_d(T a, T b, T* ga, T* gb) {
+  const T s = T(0.5) * (sgn(a) + sgn(b));
+  const T aa = Num<T>::abs_(a), ab = Num<T>::abs_(b);
+  const T wa = wmin(aa, ab), wb = wmin(ab, aa);
+  *ga = s * wa * sgn(a);
+  *gb = s * wb * sgn(b);
+}
+
+// |v|^2 as the forward forms it (abs_velocity squared)
+template <typename T, int DIM>
+__device__ __forceinline__ T vsq(const T* q) {
+  const T u = abs_velocity<T, DIM>(q);
+  return u * u;
+}
+
+// ------------------------------------------------------------ pointwise VJPs
+
+// lq += (dU/dq)^T lU for U = prim_to_cons(q)
+template <typename T, int DIM>
+__device__ __forceinline__ void prim_to_cons_vjp(const T* q, const T* lU, T gamma, T* lq) {
+  constexpr int E = DIM + 1;
+  const T rho = q[0];
+  T r = lU[0] + lU[E] * T(0.5) * vsq<T, DIM>(q);
+#pragma unroll
+  for (int a = 1; a <= DIM; ++a) {
+    r += lU[a] * q[a];
+    lq[a] += lU[a] * rho + lU[E] * rho * q[a];
+  }
+  lq[0] += r;
+  lq[E] += lU[E] / (gamma - T(1));
+}
+
+// lU = (dq/dU)^T lq for q = cons_to_prim(U)
+template <typename T, int DIM>
+__device__ __forceinline__ void cons_to_prim_vjp(const T* U, const T* lq, T gamma, T* lU) {
+  constexpr int E = DIM + 1;
+  const T rho = U[0];
+  T q[DIM + 2];
+  cons_to_prim<T, DIM>(U, q, gamma);
+  // p = (gamma - 1) rho e, e = E / rho - |v|^2 / 2
+  const T e = U[E] / rho - T(0.5) * vsq<T, DIM>(q);
+  const T le = lq[E] * (gamma - T(1)) * rho;
+  T lrho = lq[0] + lq[E] * (gamma - T(1)) * e - le * U[E] / (rho * rho);
+  lU[E] = le / rho;
+#pragma unroll
+  for (int a = 1; a <= DIM; ++a) {
+    const T lv = lq[a] - le * q[a];  // |v|^2 enters e with -1/2
+    lU[a] = lv / rho;
+    lrho -= lv * q[a] / rho;
+  }
+  lU[0] = lrho;
+}
+
+// lq += (dF/dq)^T lF for F = euler_flux(q, d)
+template <typename T, int DIM>
+__device__ __forceinline__ void euler_flux_vjp(const T* q, int d, T gamma, const T* lF, T* lq) {
+  constexpr int E = DIM + 1;
+  const T rho = q[0], p = q[E], ud = q[d];
+  const T v2 = vsq<T, DIM>(q);
+  const T En = total_energy(rho, abs_velocity<T, DIM>(q), p, gamma);
+  T lrho = lF[0] * ud + lF[E] * ud * T(0.5) * v2;
+  T lud = lF[0] * rho + lF[E] * (p + En);
+#pragma unroll
+  for (int a = 1; a <= DIM; ++a) {
+    lrho += lF[a] * ud * q[a];
+    lud += lF[a] * q[a] * rho;
+    lq[a] += lF[a] * ud * rho + lF[E] * ud * rho * q[a];
+  }
+  lq[0] += lrho;
+  lq[d] += lud;
+  lq[E] += lF[d] + lF[E] * ud * (T(1) + T(1) / (gamma - T(1)));
+}
+
+// (lqL, lqR) += VJP of the HLL flux (hll.py:36-109)
+template <typename T, int DIM>
+__device__ __forceinline__ void hll_vjp(const T* qL, const T* qR, int d, T gamma, const T* lF, T* lqL, T* lqR) {
+  constexpr int NV = DIM + 2, E = DIM + 1;
+  const T rhoL = qL[0], rhoR = qR[0], pL = qL[E], pR = qR[E];
+  const T uL = qL[d], uR = qR[d];
+  const T cL = sound_speed(rhoL, pL, gamma), cR = sound_speed(rhoR, pR, gamma);
+  T FL[NV], FR[NV], UL[NV], UR[NV];
+  euler_flux<T, DIM>(qL, d, gamma, FL);
+  euler_flux<T, DIM>(qR, d, gamma, FR);
+  prim_to_cons<T, DIM>(qL, UL, gamma);
+  prim_to_cons<T, DIM>(qR, UR, gamma);
+  const T a1 = uL + cL, a2 = uR + cR, b1 = uL - cL, b2 = uR - cR;
+  const T ma = jmax(a1, a2), mb = jmin(b1, b2);
+  const T SR = jmax(ma, T(0)), SL = jmin(mb, T(0));
+  const T den = SR - SL;
+  T lnum[NV], lFL[NV], lFR[NV], lUL[NV], lUR[NV];
+  T lden = T(0), lSR = T(0), lSL = T(0);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const T num = SR * FL[v] - SL * FR[v] + SL * SR * (UR[v] - UL[v]);
+    lnum[v] = lF[v] / den;
+    lden -= lF[v] * (num / den) / den;
+    lFL[v] = SR * lnum[v];
+    lFR[v] = -SL * lnum[v];
+    lUR[v] = SL * SR * lnum[v];
+    lUL[v] = -lUR[v];
+    lSR += lnum[v] * (FL[v] + SL * (UR[v] - UL[v]));
+    lSL += lnum[v] * (-FR[v] + SR * (UR[v] - UL[v]));
+  }
+  lSR += lden;
+  lSL -= lden;
+  // SR = max(max(a1, a2), 0), SL = min(min(b1, b2), 0)
+  const T lma = lSR * wmax(ma, T(0)), lmb = lSL * wmin(mb, T(0));
+  const T la1 = lma * wmax(a1, a2), la2 = lma * wmax(a2, a1);
+  const T lb1 = lmb * wmin(b1, b2), lb2 = lmb * wmin(b2, b1);
+  const T lcL = la1 - lb1, lcR = la2 - lb2;
+  lqL[d] += la1 + lb1;
+  lqR[d] += la2 + lb2;
+  // c = sqrt(gamma p / rho)
+  const T kL = lcL * T(0.5) / cL * gamma / rhoL, kR = lcR * T(0.5) / cR * gamma / rhoR;
+  lqL[E] += kL;
+  lqL[0] -= kL * pL / rhoL;
+  lqR[E] += kR;
+  lqR[0] -= kR * pR / rhoR;
+  euler_flux_vjp<T, DIM>(qL, d, gamma, lFL, lqL);
+  euler_flux_vjp<T, DIM>(qR, d, gamma, lFR, lqR);
+  prim_to_cons_vjp<T, DIM>(qL, lUL, gamma, lqL);
+  prim_to_cons_vjp<T, DIM>(qR, lUR, gamma, lqR);
+}
+
+// ------------------------------------------------------------ kernels
+
+template <typename T>
+struct AdjGrid {
+  int n;
+  long long nc;
+  double dx;
+  double gamma;
+};
+
+template <int DIM>
+__device__ __forceinline__ void decompose(long long c, int n, int* ic) {
+  if (DIM == 2) { ic[0] = (int)(c / n); ic[1] = (int)(c % n); ic[2] = 0; }
+  else { ic[2] = (int)(c % n); ic[1] = (int)((c / n) % n); ic[0] = (int)(c / ((long long)n * n)); }
+}
+
+template <int DIM>
+__device__ __forceinline__ long long shifted(const int* ic, int k, int off, int n) {
+  int j[3] = {ic[0], ic[1], ic[2]};
+  j[k] = wrap(j[k] + off, n);
+  return cell_index<DIM>(j[0], j[1], j[2], n);
+}
+
+// Pointwise part of a hydro stage's adjoint.  P_out = prim(U) (P0 null) or
+// P_out = prim((cons(P0) + cons(prim(U))) / 2).  Writes lU (the cotangent of
+// U = cons(P_in) + flux terms) and sets (or, with `accumulate`, adds)
+// lPin = (d cons(P_in))^T lU; adds the P0 term into lP0.  lPout may alias
+// lPin (each cell reads before it writes).
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kThreads)
+k_stage_point(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lPout, T* lU, T* lPin, T* lP0,
+              int accumulate) {
+  constexpr int NV = DIM + 2;
+  const long long nc = g.nc;
+  const T gamma = T(g.gamma);
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+       c += (long long)gridDim.x * blockDim.x) {
+    T q[NV], U[NV], lq[NV], lu[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) { q[v] = Pout[v * nc + c]; lq[v] = lPout[v * nc + c]; }
+    prim_to_cons<T, DIM>(q, U, gamma);
+    cons_to_prim_vjp<T, DIM>(U, lq, gamma, lu);
+    if (P0) {
+      T q0[NV], l0[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        lu[v] = T(0.5) * lu[v];
+        q0[v] = P0[v * nc + c];
+        l0[v] = T(0);
+      }
+      prim_to_cons_vjp<T, DIM>(q0, lu, gamma, l0);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) lP0[v * nc + c] += l0[v];
+    }
+    T qi[NV], li[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) { qi[v] = Pin[v * nc + c]; li[v] = T(0); }
+    prim_to_cons_vjp<T, DIM>(qi, lu, gamma, li);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      lU[v * nc + c] = lu[v];
+      lPin[v * nc + c] = accumulate ? lPin[v * nc + c] + li[v] : li[v];
+    }
+  }
+}
+
+// Line tiles of the flux adjoint along axis K: L cells along K by W lines
+// along J (the contiguous axis when K is not, else the next-to-last axis).
+template <int DIM, int K>
+struct AxisTile {
+  static constexpr bool KFAST = (K == DIM - 1);
+  static constexpr int L = KFAST ? 32 : 8;
+  static constexpr int W = KFAST ? 8 : 32;
+  static constexpr int J = KFAST ? DIM - 2 : DIM - 1;
+  static constexpr int M = 3 - K - J;  // third axis (3D only)
+  static constexpr int PL = L + 6, UL = L + 4, DL = L + 4, FL = L + 3;
+  template <typename T>
+  static constexpr size_t smem(int nv) {
+    return sizeof(T) * (size_t)nv * W * (PL + UL + 3 * DL + 2 * FL);
+  }
+};
+
+// lPin += the flux terms of one axis: for every face f (between cells f-1
+// and f) of the tile and its reach, the cotangent of the HLL flux
+// lF = dt/dx (lU[f] - lU[f-1]) is pulled back through the flux and the
+// limited reconstruction qL = P[f-1] + D[f-1], qR = P[f] - D[f],
+// D[m] = minmod((P[m] - P[m-1]) / dx, (P[m+1] - P[m]) / dx) dx / 2
+// (reconstruction.py:399-431, limited_gradients.py:22-88), and every cell of
+// the tile gathers the faces that read it (f in [m-1, m+2]).
+template <typename T, int DIM, int K>
+__global__ void __launch_bounds__(kThreads)
+k_stage_axis(AdjGrid<T> g, const T* Pin, const T* lU, T* lPin, T h) {
+  using A = AxisTile<DIM, K>;
+  constexpr int NV = DIM + 2, L = A::L, W = A::W;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sP = reinterpret_cast<T*>(smem_raw);   // [NV][W][PL], cell m at m + 3
+  T* sU = sP + NV * W * A::PL;              // [NV][W][UL], cell m at m + 2
+  T* sD = sU + NV * W * A::UL;              // [NV][W][DL] slopes, m at m + 2
+  T* sGa = sD + NV * W * A::DL;             // d minmod / d backward difference
+  T* sGb = sGa + NV * W * A::DL;
+  T* sLL = sGb + NV * W * A::DL;            // [NV][W][FL] cotangent of qL, face f at f + 1
+  T* sLR = sLL + NV * W * A::FL;
+  const int n = g.n;
+  const long long nc = g.nc;
+  const T gamma = T(g.gamma);
+  const T dxT = T(g.dx);
+  const T inv_dx = T(1.0 / g.dx);
+
+  // tile origin
+  const int tK = (n + L - 1) / L, tJ = (n + W - 1) / W;
+  long long b = blockIdx.x;
+  const int bK = (int)(b % tK);
+  b /= tK;
+  const int bJ = (int)(b % tJ);
+  b /= tJ;
+  const int oK = bK * L, oJ = bJ * W, oM = (DIM == 3) ? (int)b : 0;
+
+  auto cell = [&](int l, int w) -> long long {  // l may be outside [0, L): periodic along K
+    int ic[3] = {0, 0, 0};
+    ic[K] = ((oK + l) % n + n) % n;
+    ic[A::J] = oJ + w;
+    if (DIM == 3) ic[A::M] = oM;
+    return cell_index<DIM>(ic[0], ic[1], ic[2], n);
+  };
+
+  // loads: P for m in [-3, L+2], lU for m in [-2, L+1]
+  for (int e = threadIdx.x; e < W * A::PL; e += blockDim.x) {
+    const int w = e / A::PL, m = e % A::PL - 3;
+    if (oJ + w >= n) continue;
+    const long long c = cell(m, w);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sP[(v * W + w) * A::PL + m + 3] = Pin[v * nc + c];
+  }
+  for (int e = threadIdx.x; e < W * A::UL; e += blockDim.x) {
+    const int w = e / A::UL, m = e % A::UL - 2;
+    if (oJ + w >= n) continue;
+    const long long c = cell(m, w);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sU[(v * W + w) * A::UL + m + 2] = lU[v * nc + c];
+  }
+  __syncthreads();
+  // slopes and their derivative weights for m in [-2, L+1]
+  for (int e = threadIdx.x; e < W * A::DL; e += blockDim.x) {
+    const int w = e / A::DL, m = e % A::DL - 2;
+    if (oJ + w >= n) continue;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const T* s = sP + (v * W + w) * A::PL + m + 3;
+      const T bd = (s[0] - s[-1]) / dxT, fd = (s[1] - s[0]) / dxT;
+      T ga, gb;
+      minmod_d(bd, fd, &ga, &gb);
+      const int o = (v * W + w) * A::DL + m + 2;
+      sD[o] = limited(bd, fd, 0, dxT) * dxT / T(2);
+      sGa[o] = ga;
+      sGb[o] = gb;
+    }
+  }
+  __syncthreads();
+  // faces f in [-1, L+1]
+  for (int e = threadIdx.x; e < W * A::FL; e += blockDim.x) {
+    const int w = e / A::FL, f = e % A::FL - 1;
+    if (oJ + w >= n) continue;
+    T qL[NV], qR[NV], lF[NV], lL[NV], lR[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const T* s = sP + (v * W + w) * A::PL + 3;
+      const T* dd = sD + (v * W + w) * A::DL + 2;
+      qL[v] = s[f - 1] + dd[f - 1];
+      qR[v] = s[f] - dd[f];
+      const T* u = sU + (v * W + w) * A::UL + 2;
+      // U[i] += inv_dx (F[i-1/2] - F[i+1/2]) h: face f feeds cell f (+) and f - 1 (-)
+      lF[v] = inv_dx * (u[f] - u[f - 1]) * h;
+      lL[v] = T(0);
+      lR[v] = T(0);
+    }
+    hll_vjp<T, DIM>(qL, qR, K + 1, gamma, lF, lL, lR);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      sLL[(v * W + w) * A::FL + f + 1] = lL[v];
+      sLR[(v * W + w) * A::FL + f + 1] = lR[v];
+    }
+  }
+  __syncthreads();
+  // cells of the tile
+  for (int e = threadIdx.x; e < W * L; e += blockDim.x) {
+    int w, l;
+    if (A::KFAST) { l = e % L; w = e / L; } else { w = e % W; l = e / W; }
+    if (oJ + w >= n || oK + l >= n) continue;
+    const long long c = cell(l, w);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const T* LL = sLL + (v * W + w) * A::FL + 1;
+      const T* LR = sLR + (v * W + w) * A::FL + 1;
+      const T* Ga = sGa + (v * W + w) * A::DL + 2;
+      const T* Gb = sGb + (v * W + w) * A::DL + 2;
+      // cotangent of the slope D[m] = lqL[m+1] - lqR[m]
+      const T dm1 = LL[l] - LR[l - 1], d0 = LL[l + 1] - LR[l], dp1 = LL[l + 2] - LR[l + 1];
+      const T r = LL[l + 1] + LR[l] + d0 * (Ga[l] - Gb[l]) / T(2) - dp1 * Ga[l + 1] / T(2) +
+                  dm1 * Gb[l - 1] / T(2);
+      lPin[v * nc + c] += r;
+    }
+  }
+}
+
+// ---- magnetic map
+
+// iterate (B, v) at cell c: from the iterate buffer, or (first evaluation)
+// B0 and v0 (vz = 0 in 2D)
+template <typename T, int DIM>
+__device__ __forceinline__ void load_Z(const T* Z, const T* S, long long c, long long nc, T* B, T* v) {
+  if (Z) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { B[i] = Z[i * nc + c]; v[i] = Z[(3 + i) * nc + c]; }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) B[i] = S[(DIM + 2 + i) * nc + c];
+    v[0] = S[nc + c];
+    v[1] = S[2 * nc + c];
+    v[2] = (DIM == 3) ? S[3 * nc + c] : T(0);
+  }
+}
+
+template <typename T, int DIM>
+__device__ __forceinline__ void load_B0v0(const T* S, long long c, long long nc, T* B, T* v) {
+  load_Z<T, DIM>(nullptr, S, c, nc, B, v);
+}
+
+// averaged fields at c (midpoint) or the iterate (Euler)
+template <typename T, int DIM>
+__device__ __forceinline__ void avg_at(const T* Z, const T* S, long long c, long long nc, bool midpoint, T* Ba,
+                                       T* va) {
+  T Bk[3], vk[3], B0[3], v0[3];
+  load_Z<T, DIM>(Z, S, c, nc, Bk, vk);
+  load_B0v0<T, DIM>(S, c, nc, B0, v0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    Ba[i] = midpoint ? (Bk[i] + B0[i]) / T(2) : Bk[i];
+    va[i] = midpoint ? (vk[i] + v0[i]) / T(2) : vk[i];
+  }
+}
+
+// curl by central differences of a 3-vector field given per neighbour
+// (Fp[k] = F at c + e_k, Fm[k] = F at c - e_k), _vector_maths.py:55-100
+template <typename T, int DIM>
+__device__ __forceinline__ void curl_c(T (*Fp)[3], T (*Fm)[3], T dx, T* out) {
+  auto D = [&](int i, int k) { return T(0.5) * (Fp[k][i] - Fm[k][i]) / dx; };
+  if (DIM == 2) {
+    out[0] = D(2, 1);
+    out[1] = -D(2, 0);
+    out[2] = D(1, 0) - D(0, 1);
+  } else {
+    out[0] = D(2, 1) - D(1, 2);
+    out[1] = D(0, 2) - D(2, 0);
+    out[2] = D(1, 0) - D(0, 1);
+  }
+}
+
+// Pass 1 of the adjoint of one evaluation (B', v') = G(Z) with
+// B' = B0 - h curl(Ba x va), v' = v0 - h (Ba x curl Ba) / rho:
+//   lE = -h curl(lB')   (the central-difference curl is its own transpose
+//                        on a periodic grid)
+//   lX = -h lv' / rho,  lrho += h lv'.X / rho^2
+//   lBa = va x lE + J x lX (+ curl(lJ) in pass 2), lva = lE x Ba, lJ = lX x Ba
+// and lB0 += lB', lv0 += lv'.  Writes lJ, the partial lBa and lva.
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kThreads)
+k_mag_adj1(AdjGrid<T> g, const T* Z, const T* S, const T* lZn, T h, int midpoint, T* lJ, T* lBa, T* lva,
+           T* lB0, T* lv0, T* lrho) {
+  const long long nc = g.nc;
+  const int n = g.n;
+  const T dx = T(g.dx);
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+       c += (long long)gridDim.x * blockDim.x) {
+    int ic[3];
+    decompose<DIM>(c, n, ic);
+    T Ba[3], va[3];
+    avg_at<T, DIM>(Z, S, c, nc, midpoint != 0, Ba, va);
+    T Bp[3][3], Bm[3][3], Lp[3][3], Lm[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Bp[k][i] = Bm[k][i] = Lp[k][i] = Lm[k][i] = T(0);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      T vv[3];
+      const long long cp = shifted<DIM>(ic, k, +1, n), cm = shifted<DIM>(ic, k, -1, n);
+      avg_at<T, DIM>(Z, S, cp, nc, midpoint != 0, Bp[k], vv);
+      avg_at<T, DIM>(Z, S, cm, nc, midpoint != 0, Bm[k], vv);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) { Lp[k][i] = lZn[i * nc + cp]; Lm[k][i] = lZn[i * nc + cm]; }
+    }
+    T J[3], lE[3];
+    curl_c<T, DIM>(Bp, Bm, dx, J);
+    curl_c<T, DIM>(Lp, Lm, dx, lE);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) lE[i] = -h * lE[i];
+    T X[3];
+    cross3(Ba, J, X);
+    const T rho = S[c];
+    T lX[3], lvn[3];
+    T lr = T(0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      lvn[i] = lZn[(3 + i) * nc + c];
+      lX[i] = -h * lvn[i] / rho;
+      lr += h * lvn[i] * X[i] / (rho * rho);
+    }
+    T t1[3], t2[3], lvA[3], lJc[3];
+    cross3(va, lE, t1);
+    cross3(J, lX, t2);
+    cross3(lE, Ba, lvA);
+    cross3(lX, Ba, lJc);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      lJ[i * nc + c] = lJc[i];
+      lBa[i * nc + c] = t1[i] + t2[i];
+      lva[i * nc + c] = lvA[i];
+      lB0[i * nc + c] += lZn[i * nc + c];
+      lv0[i * nc + c] += lvn[i];
+    }
+    lrho[c] += lr;
+  }
+}
+
+// Pass 2: lBa += curl(lJ); then Ba = (Bk + B0)/2 (or Bk) hands lBa, lva to
+// the iterate (lZ, or B0 / v0 for the first evaluation) and to B0 / v0.
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kThreads)
+k_mag_adj2(AdjGrid<T> g, const T* lJ, const T* lBa, const T* lva, int midpoint, int first, T* lZ, T* lB0,
+           T* lv0) {
+  const long long nc = g.nc;
+  const int n = g.n;
+  const T dx = T(g.dx);
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+       c += (long long)gridDim.x * blockDim.x) {
+    int ic[3];
+    decompose<DIM>(c, n, ic);
+    T Lp[3][3], Lm[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Lp[k][i] = Lm[k][i] = T(0);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      const long long cp = shifted<DIM>(ic, k, +1, n), cm = shifted<DIM>(ic, k, -1, n);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) { Lp[k][i] = lJ[i * nc + cp]; Lm[k][i] = lJ[i * nc + cm]; }
+    }
+    T cJ[3];
+    curl_c<T, DIM>(Lp, Lm, dx, cJ);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const T lb = lBa[i * nc + c] + cJ[i];
+      const T lv = lva[i * nc + c];
+      const T bk = midpoint ? lb / T(2) : lb, vk = midpoint ? lv / T(2) : lv;
+      const T b0 = midpoint ? lb / T(2) : T(0), v0 = midpoint ? lv / T(2) : T(0);
+      if (first) {
+        lB0[i * nc + c] += bk + b0;
+        lv0[i * nc + c] += vk + v0;
+      } else {
+        lZ[i * nc + c] = bk;
+        lZ[(3 + i) * nc + c] = vk;
+        lB0[i * nc + c] += b0;
+        lv0[i * nc + c] += v0;
+      }
+    }
+  }
+}
+
+// Adjoint of the write-back S3 = W(S2, Z) (_magnetic_field_update.py:208-242):
+// rho and p pass through (the refresh is the identity on p), the velocity
+// and B rows of S3 come from the final iterate Z.  Sets lS2's density and
+// pressure rows and zeroes its velocity and B rows (they accumulate the
+// magnetic iterations' cotangents of v0 and B0); sets lZ.
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kThreads)
+k_final_adj(AdjGrid<T> g, const T* lS3, T* lZ, T* lS2, T* lv0) {
+  const long long nc = g.nc;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+       c += (long long)gridDim.x * blockDim.x) {
+    lS2[c] = lS3[c];
+    lS2[(DIM + 1) * nc + c] = lS3[(DIM + 1) * nc + c];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) lS2[(1 + i) * nc + c] = T(0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      lS2[(DIM + 2 + i) * nc + c] = T(0);
+      lZ[i * nc + c] = lS3[(DIM + 2 + i) * nc + c];
+      lZ[(3 + i) * nc + c] = (i < DIM) ? lS3[(1 + i) * nc + c] : T(0);
+      lv0[i * nc + c] = T(0);
+    }
+  }
+}
+
+// lS2's velocity rows += lv0 (the z row of lv0 is the synthesised vz = 0 in 2D)
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kThreads)
+k_add_v0(AdjGrid<T> g, const T* lv0, T* lS2) {
+  const long long nc = g.nc;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
+       c += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int i = 0; i < DIM; ++i) lS2[(1 + i) * nc + c] += lv0[i * nc + c];
+  }
+}
+
+// ---- tape kernels (forward pieces with a given dt; same per-item code as the step)
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kFVThreads)
+k_tape_stage(FVArgs<T> a, const T* Pin, T* Pout, const T* P0, T h) {
+  using G = TileGeom<T, DIM>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
+  const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
+  double m[3] = {0.0, 0.0, 0.0};
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int o[3];
+    tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
+    FVItems<T, DIM, RS_HLL, 0>::hydro(a, o, Pin, Pout, P0, h, nullptr, smem, m, false);
+  }
+}
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kFVThreads)
+k_tape_mag(FVArgs<T> a, const T* Z, T* Zn, T h) {
+  const long long nc = a.ncells;
+  MagSrc<T, DIM> src = Z ? MagSrc<T, DIM>{Z, Z + 3 * nc, false}
+                         : MagSrc<T, DIM>{a.state + (DIM + 2) * nc, a.state + nc, true};
+  T change = T(0);
+  MagItems<T, DIM>::direct(a, src, Zn, h, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
+                           (long long)gridDim.x * blockDim.x, &change);
+}
+
+template <typename T, int DIM>
+__global__ void __launch_bounds__(kFVThreads)
+k_tape_final(FVArgs<T> a, const T* Z) {
+  double m[3] = {0.0, 0.0, 0.0};
+  MagItems<T, DIM>::finalize(a, Z, (long long)blockIdx.x * blockDim.x + threadIdx.x, a.ncells,
+                             (long long)gridDim.x * blockDim.x, false, m);
+}
+
+// ------------------------------------------------------------ host side
+
+// One step's slots in the tape: S0 (full state), S1 (gas), S2 (full), the
+// iterates Z[0..k] (6 rows each), S3 (full), S4 (gas); S5 is the next
+// step's S0.
+template <typename T>
+struct StepTape {
+  T* S0;
+  T* S1;
+  T* S2;
+  T* Z;   // Z[j] = Z + 6 j nc
+  T* S3;
+  T* S4;
+  T* S5;
+  int iters;  // k: evaluations after the first
+  double dt;
+};
+
+// Cotangent buffers of one reverse step.
+template <typename T>
+struct AdjScratch {
+  T* lS4;   // gas rows
+  T* lS3;   // full
+  T* lS2;   // full
+  T* lS1;   // gas
+  T* lU;    // gas
+  T* lZ0;   // 6 rows
+  T* lZ1;
+  T* lJ;    // 3
+  T* lBa;   // 3
+  T* lva;   // 3
+  T* lv0;   // 3
+};
+
+inline int grid_for(long long nc) {
+  const long long b = (nc + kThreads - 1) / kThreads;
+  return (int)(b < 4096 ? b : 4096);
+}
+
+template <typename T, int DIM>
+int set_attrs() {
+  constexpr int NV = DIM + 2;
+  int rc = 0;
+  rc |= (int)cudaFuncSetAttribute(k_stage_axis<T, DIM, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)AxisTile<DIM, 0>::template smem<T>(NV));
+  rc |= (int)cudaFuncSetAttribute(k_stage_axis<T, DIM, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)AxisTile<DIM, 1>::template smem<T>(NV));
+  if (DIM == 3)
+    rc |= (int)cudaFuncSetAttribute(k_stage_axis<T, DIM, DIM - 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)AxisTile<DIM, DIM - 1>::template smem<T>(NV));
+  rc |= (int)cudaFuncSetAttribute(k_tape_stage<T, DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)TileGeom<T, DIM>::SMEM);
+  return rc ? AMX_ERR_CUDA : AMX_OK;
+}
+
+template <typename T, int DIM, int K>
+void launch_axis(const AdjGrid<T>& g, const T* Pin, const T* lU, T* lPin, T h, cudaStream_t s) {
+  using A = AxisTile<DIM, K>;
+  const long long blocks = (long long)((g.n + A::L - 1) / A::L) * ((g.n + A::W - 1) / A::W) * (DIM == 3 ? g.n : 1);
+  k_stage_axis<T, DIM, K><<<(unsigned)blocks, kThreads, A::template smem<T>(DIM + 2), s>>>(g, Pin, lU, lPin, h);
+}
+
+// Reverse of one hydro stage: lPout -> lPin (set, or added with
+// `accumulate`), and the RK2 combination's P0 term into lP0.
+template <typename T, int DIM>
+void stage_adjoint(const AdjGrid<T>& g, const T* Pin, const T* Pout, const T* P0, const T* lPout, T* lU, T* lPin,
+                   T* lP0, int accumulate, T h, cudaStream_t s) {
+  k_stage_point<T, DIM><<<grid_for(g.nc), kThreads, 0, s>>>(g, Pin, Pout, P0, lPout, lU, lPin, lP0, accumulate);
+  launch_axis<T, DIM, 0>(g, Pin, lU, lPin, h, s);
+  launch_axis<T, DIM, 1>(g, Pin, lU, lPin, h, s);
+  if (DIM == 3) launch_axis<T, DIM, DIM - 1>(g, Pin, lU, lPin, h, s);
+}
+
+// Records one step of the forward (dt, k given) into `t`; S0 is filled.
+template <typename T, int DIM>
+int tape_step(FVArgs<T> a, const StepTape<T>& t, bool mhd, cudaStream_t s) {
+  using G = TileGeom<T, DIM>;
+  constexpr int NVG = DIM + 2;
+  const long long nc = a.ncells;
+  const int nvt = NVG + (mhd ? 3 : 0);
+  const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
+  const unsigned tiles = (unsigned)ntiles;
+  const T dtT = T(t.dt);
+  const T h = mhd ? dtT / T(2) : dtT;
+  k_tape_stage<T, DIM><<<tiles, kFVThreads, G::SMEM, s>>>(a, t.S0, t.S1, nullptr, h);
+  T* S2 = mhd ? t.S2 : t.S5;
+  // S2 = S0 with the gas rows replaced
+  if (mhd && cudaMemcpyAsync(S2 + NVG * nc, t.S0 + NVG * nc, sizeof(T) * 3 * nc, cudaMemcpyDeviceToDevice, s))
+    return AMX_ERR_CUDA;
+  k_tape_stage<T, DIM><<<tiles, kFVThreads, G::SMEM, s>>>(a, t.S1, S2, t.S0, h);
+  if (!mhd) return cudaGetLastError() == cudaSuccess ? AMX_OK : AMX_ERR_CUDA;
+  FVArgs<T> am = a;
+  am.state = S2;
+  const int gb = grid_for(nc);
+  for (int j = 0; j <= t.iters; ++j)
+    k_tape_mag<T, DIM><<<gb, kFVThreads, 0, s>>>(am, j ? t.Z + 6 * (j - 1) * nc : nullptr, t.Z + 6 * j * nc, dtT);
+  if (cudaMemcpyAsync(t.S3, S2, sizeof(T) * nvt * nc, cudaMemcpyDeviceToDevice, s)) return AMX_ERR_CUDA;
+  FVArgs<T> af = a;
+  af.state = t.S3;
+  k_tape_final<T, DIM><<<gb, kFVThreads, 0, s>>>(af, t.Z + 6 * t.iters * nc);
+  k_tape_stage<T, DIM><<<tiles, kFVThreads, G::SMEM, s>>>(a, t.S3, t.S4, nullptr, h);
+  if (cudaMemcpyAsync(t.S5 + NVG * nc, t.S3 + NVG * nc, sizeof(T) * 3 * nc, cudaMemcpyDeviceToDevice, s))
+    return AMX_ERR_CUDA;
+  k_tape_stage<T, DIM><<<tiles, kFVThreads, G::SMEM, s>>>(a, t.S4, t.S5, t.S3, h);
+  return cudaGetLastError() == cudaSuccess ? AMX_OK : AMX_ERR_CUDA;
+}
+
+// Reverse of one step: lam (cotangent of S5, full state) -> lS0 (full state).
+// lam and lS0 may not alias.
+template <typename T, int DIM>
+int adjoint_step(const AdjGrid<T>& g, const StepTape<T>& t, bool mhd, int midpoint, const T* lam, T* lS0,
+                 const AdjScratch<T>& w, cudaStream_t s) {
+  constexpr int NVG = DIM + 2;
+  const long long nc = g.nc;
+  const size_t row = sizeof(T) * (size_t)nc;
+  const T dtT = T(t.dt);
+  const T h = mhd ? dtT / T(2) : dtT;
+  if (!mhd) {
+    if (cudaMemsetAsync(lS0, 0, row * NVG, s)) return AMX_ERR_CUDA;
+    stage_adjoint<T, DIM>(g, t.S1, t.S5, t.S0, lam, w.lU, w.lS1, lS0, 0, h, s);
+    stage_adjoint<T, DIM>(g, t.S0, t.S1, nullptr, w.lS1, w.lU, lS0, nullptr, 1, h, s);
+    return cudaGetLastError() == cudaSuccess ? AMX_OK : AMX_ERR_CUDA;
+  }
+  const int gb = grid_for(nc);
+  // second half: S5 = C(S3, L(S4)), S4 = L(S3); B rows of S3 pass to S5
+  if (cudaMemsetAsync(w.lS3, 0, row * NVG, s)) return AMX_ERR_CUDA;
+  if (cudaMemcpyAsync(w.lS3 + NVG * nc, lam + NVG * nc, row * 3, cudaMemcpyDeviceToDevice, s)) return AMX_ERR_CUDA;
+  stage_adjoint<T, DIM>(g, t.S4, t.S5, t.S3, lam, w.lU, w.lS4, w.lS3, 0, h, s);
+  stage_adjoint<T, DIM>(g, t.S3, t.S4, nullptr, w.lS4, w.lU, w.lS3, nullptr, 1, h, s);
+  // write-back and the fixed-point evaluations, last to first
+  k_final_adj<T, DIM><<<gb, kThreads, 0, s>>>(g, w.lS3, w.lZ0, w.lS2, w.lv0);
+  T* lZn = w.lZ0;
+  T* lZp = w.lZ1;
+  T* lB0 = w.lS2 + NVG * nc;
+  for (int j = t.iters; j >= 0; --j) {
+    const T* Zin = j ? t.Z + 6 * (j - 1) * nc : nullptr;
+    k_mag_adj1<T, DIM><<<gb, kThreads, 0, s>>>(g, Zin, t.S2, lZn, dtT, midpoint, w.lJ, w.lBa, w.lva, lB0, w.lv0,
+                                               w.lS2);
+    k_mag_adj2<T, DIM><<<gb, kThreads, 0, s>>>(g, w.lJ, w.lBa, w.lva, midpoint, j == 0, lZp, lB0, w.lv0);
+    T* tmp = lZn; lZn = lZp; lZp = tmp;
+  }
+  k_add_v0<T, DIM><<<gb, kThreads, 0, s>>>(g, w.lv0, w.lS2);
+  // first half: S2 = C(S0, L(S1)), S1 = L(S0); B rows of S0 pass to S2
+  if (cudaMemsetAsync(lS0, 0, row * NVG, s)) return AMX_ERR_CUDA;
+  if (cudaMemcpyAsync(lS0 + NVG * nc, lB0, row * 3, cudaMemcpyDeviceToDevice, s)) return AMX_ERR_CUDA;
+  stage_adjoint<T, DIM>(g, t.S1, t.S2, t.S0, w.lS2, w.lU, w.lS1, lS0, 0, h, s);
+  stage_adjoint<T, DIM>(g, t.S0, t.S1, nullptr, w.lS1, w.lU, lS0, nullptr, 1, h, s);
+  return cudaGetLastError() == cudaSuccess ? AMX_OK : AMX_ERR_CUDA;
+}
+
+}  // namespace adj
+}  // namespace amx

@@ -251,6 +251,37 @@ int amx_batch_tiling(const amx_batch* batch, int32_t* variant, int32_t* blocks_p
 /* Forces a tiling (blocks_per_sm <= 0 picks the default). */
 int amx_batch_set_tiling(amx_batch* batch, int32_t variant, int32_t blocks_per_sm);
 
+/* ---- discrete adjoint --------------------------------------------------------- */
+
+/* Reverse-mode gradient of the FV time integration (2D / 3D, HLL, MINMOD,
+ * periodic; MHD or hydro).  The reference differentiates time_integration
+ * with jax.grad (tests/mhd_tests/mhd_correct.py:237-264): dt is held fixed
+ * (stop_gradient, astronomix/time_stepping/time_integration.py:632-661) and
+ * the magnetic fixed point is differentiated through the iterations it took
+ * (its while loop, _magnetic_field_update.py:127-171).  This is the
+ * hand-written discrete adjoint of the same program.  amx_adjoint_forward runs
+ * the ordinary kernel to t_end, keeping the state every `checkpoint_every`
+ * steps and the dt / iteration schedule; amx_adjoint_backward maps the
+ * cotangent of the final state (full state layout) to the cotangent of the
+ * initial state, replaying one segment at a time from its checkpoint.
+ * `max_steps` bounds the schedule. */
+typedef struct amx_adjoint amx_adjoint;
+int amx_adjoint_create(const amx_config* cfg, int32_t checkpoint_every, int64_t max_steps, amx_adjoint** out);
+int amx_adjoint_destroy(amx_adjoint* adj);
+/* Advances `state` in place to prm->t_end, recording checkpoints and the
+ * schedule (synchronises; fills *info when non-null). */
+int amx_adjoint_forward(amx_adjoint* adj, void* state, const amx_params* prm, amx_run_info* info, void* stream);
+/* grad_initial = (d final / d initial)^T grad_final for the last forward
+ * (device buffers in the state layout; synchronises). */
+int amx_adjoint_backward(amx_adjoint* adj, const void* grad_final, void* grad_initial, void* stream);
+/* Advances `state` in place with the recorded schedule (fixed dt and
+ * iteration counts): the program the gradient is exact for (synchronises). */
+int amx_adjoint_replay(amx_adjoint* adj, void* state, void* stream);
+/* Steps of the last forward, and the first n dt / iteration counts. */
+int amx_adjoint_schedule(amx_adjoint* adj, double* dt_host, int32_t* iters_host, int64_t n, int64_t* steps);
+/* Device bytes held for checkpoints and for the tape and cotangents. */
+int amx_adjoint_memory(const amx_adjoint* adj, size_t* checkpoint_bytes, size_t* tape_bytes);
+
 /* Library version string. */
 const char* amx_version(void);
 

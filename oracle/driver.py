@@ -26,7 +26,7 @@ from . import fd as _fd
 
 def _dtype_scalar(v, like, time_mode):
     if time_mode == "float64":
-        return float(v)
+        return xp.to_float(v)  # detached, like the reference's stop_gradient(dt)
     return xp.scalar(v, like)
 
 
