@@ -132,6 +132,8 @@ SIGNATURES = {
     "amx_adjoint_forward": (_I32, [_P, _P, ctypes.POINTER(amx_params), ctypes.POINTER(amx_run_info), _P]),
     "amx_adjoint_backward": (_I32, [_P, _P, _P, _P]),
     "amx_adjoint_replay": (_I32, [_P, _P, _P]),
+    "amx_adjoint_set_tape_budget": (_I32, [_P, ctypes.c_size_t]),
+    "amx_adjoint_uses_stored_tape": (_I32, [_P, ctypes.POINTER(_I32)]),
     "amx_adjoint_schedule": (_I32, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I32), _I64, ctypes.POINTER(_I64)]),
     "amx_adjoint_memory": (_I32, [_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     "amx_version": (ctypes.c_char_p, []),
@@ -351,6 +353,14 @@ class Adjoint:
     def backward(self, grad_final_ptr, grad_initial_ptr, stream=0):
         check(self._L.amx_adjoint_backward(self.handle, _P(grad_final_ptr), _P(grad_initial_ptr), _P(stream)),
               "amx_adjoint_backward")
+
+    def set_tape_budget(self, nbytes):
+        check(self._L.amx_adjoint_set_tape_budget(self.handle, int(nbytes)), "amx_adjoint_set_tape_budget")
+
+    def uses_stored_tape(self) -> bool:
+        y = ctypes.c_int32()
+        check(self._L.amx_adjoint_uses_stored_tape(self.handle, ctypes.byref(y)), "amx_adjoint_uses_stored_tape")
+        return bool(y.value)
 
     def replay(self, state_ptr, stream=0):
         check(self._L.amx_adjoint_replay(self.handle, _P(state_ptr), _P(stream)), "amx_adjoint_replay")

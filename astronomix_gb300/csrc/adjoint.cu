@@ -1,14 +1,19 @@
-// Checkpointed discrete adjoint of the FV time integration: host driver.
+// Discrete adjoint of the FV time integration: host driver.
 //
-// Forward: the ordinary persistent FV kernel (amx_run) advances the state
-// `checkpoint_every` steps at a time; the state at the start of every
-// segment is copied to a checkpoint, and the plan's history records every
-// step's dt and fixed-point iteration count.  Backward: the segments are
-// taken last to first; each is replayed from its checkpoint with the
-// recorded dt and iteration counts, recording every intermediate state of
-// its steps (the tape), and the adjoint kernels (adjoint.cuh) then walk its
-// steps in reverse.  The recompute is one extra forward pass; the memory is
-// the checkpoints plus one segment's tape.
+// Two ways to get the tape (every intermediate state of every step) that the
+// adjoint kernels (adjoint.cuh) walk in reverse:
+//
+// * Stored tape: when a tape budget is set and the run fits in it, the
+//   persistent FV kernel itself writes the tape during the forward pass
+//   (tape mode, fv_kernels.cuh); the backward needs no recompute.
+// * Checkpoints: the ordinary persistent kernel advances the state
+//   `checkpoint_every` steps at a time and the state at the start of every
+//   segment is kept; the backward takes the segments last to first and
+//   replays each from its checkpoint with the recorded dt and iteration
+//   counts to rebuild that segment's tape.  One extra forward pass, and the
+//   memory of the checkpoints plus one segment's tape.
+//
+// A stored-tape forward that runs out of room falls back to checkpoints.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -18,6 +23,11 @@
 
 #include "../../include/amx.h"
 #include "adjoint_api.h"
+
+namespace amx {
+int fv_run_tape(amx_plan* p, const amx_params* prm, void* tape, long long tape_cap, long long* tape_off,
+                int64_t max_steps, amx_run_info* info, cudaStream_t s);
+}
 
 using amx::adj::Ops;
 using amx::adj::ScratchView;
@@ -38,7 +48,14 @@ struct amx_adjoint {
   std::vector<int32_t> iters;
   int64_t steps = 0;
   bool have_forward = false;
-  // backward buffers
+  // stored tape (written by the forward)
+  size_t budget = 0;
+  unsigned char* ftape = nullptr;
+  size_t ftape_bytes = 0;
+  long long* d_tape_off = nullptr;
+  std::vector<long long> tape_off;
+  bool taped = false;
+  // replay buffers
   unsigned char* tape = nullptr;
   size_t tape_bytes = 0;
   unsigned char* scratch = nullptr;
@@ -90,6 +107,28 @@ void layout(const amx_adjoint* a, int64_t s0, int64_t s1, std::vector<TapeView>*
     }
     t.S5 = p; p += R * a->nvt;
     prev_s5 = t.S5;
+  }
+}
+
+// The stored tape's step views (layout of fv_kernels.cuh's tape mode).
+void layout_stored(const amx_adjoint* a, std::vector<TapeView>* out) {
+  const size_t E = a->elem;
+  const long long nc = a->nc;
+  out->assign((size_t)a->steps, TapeView{});
+  for (int64_t s = 0; s < a->steps; ++s) {
+    TapeView& t = (*out)[(size_t)s];
+    t.dt = a->dt[(size_t)s];
+    t.iters = a->iters[(size_t)s];
+    unsigned char* p = a->ftape + (size_t)a->tape_off[(size_t)s] * E;
+    t.S0 = p; p += E * nc * a->nvt;
+    t.S1 = p; p += E * nc * a->nvg;
+    if (a->cfg.mhd) {
+      t.S2 = p; p += E * nc * a->nvt;
+      t.Z = p; p += E * nc * 6 * (size_t)(t.iters + 1);
+      t.S3 = p; p += E * nc * a->nvt;
+      t.S4 = p;
+    }
+    t.S5 = a->ftape + (size_t)a->tape_off[(size_t)s + 1] * E;
   }
 }
 
@@ -160,9 +199,22 @@ int amx_adjoint_create(const amx_config* cfg, int32_t checkpoint_every, int64_t 
   return AMX_OK;
 }
 
+int amx_adjoint_set_tape_budget(amx_adjoint* a, size_t bytes) {
+  if (!a) return AMX_ERR_INVALID_ARG;
+  a->budget = bytes;
+  if (a->ftape && a->ftape_bytes != bytes) {
+    cudaFree(a->ftape);
+    a->ftape = nullptr;
+    a->ftape_bytes = 0;
+  }
+  return AMX_OK;
+}
+
 int amx_adjoint_destroy(amx_adjoint* a) {
   if (!a) return AMX_OK;
   for (void* p : a->ckpt) cudaFree(p);
+  if (a->ftape) cudaFree(a->ftape);
+  if (a->d_tape_off) cudaFree(a->d_tape_off);
   if (a->tape) cudaFree(a->tape);
   if (a->scratch) cudaFree(a->scratch);
   if (a->plan) amx_plan_destroy(a->plan);
@@ -175,10 +227,46 @@ int amx_adjoint_forward(amx_adjoint* a, void* state, const amx_params* prm, amx_
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   a->prm = *prm;
   a->have_forward = false;
+  a->taped = false;
   int rc = amx_plan_reset(a->plan, stream);
   if (rc) return rc;
   const size_t bytes = (size_t)a->nc * a->elem * a->nvt;
   amx_run_info inf{};
+  if (a->budget >= 3 * bytes) {
+    if (!a->ftape) {
+      if (cudaMalloc(&a->ftape, a->budget) != cudaSuccess) return AMX_ERR_CUDA;
+      a->ftape_bytes = a->budget;
+    }
+    if (!a->d_tape_off && cudaMalloc(&a->d_tape_off, sizeof(long long) * (size_t)(a->max_steps + 1)) != cudaSuccess)
+      return AMX_ERR_CUDA;
+    rc = cuda_ok(cudaMemsetAsync(a->d_tape_off, 0, sizeof(long long), s));
+    rc |= cuda_ok(cudaMemcpyAsync(a->ftape, state, bytes, cudaMemcpyDeviceToDevice, s));
+    if (!rc) rc = amx::fv_run_tape(a->plan, prm, a->ftape, (long long)(a->ftape_bytes / a->elem), a->d_tape_off,
+                                   a->max_steps, &inf, s);
+    if (rc) return rc;
+    if (!(inf.status & AMX_ERR_TOO_LARGE)) {
+      a->steps = inf.steps;
+      a->tape_off.assign((size_t)a->steps + 1, 0);
+      rc = cuda_ok(cudaMemcpyAsync(a->tape_off.data(), a->d_tape_off, sizeof(long long) * (a->steps + 1),
+                                   cudaMemcpyDeviceToHost, s));
+      rc |= cuda_ok(cudaStreamSynchronize(s));
+      if (rc) return rc;
+      rc = cuda_ok(cudaMemcpyAsync(state, a->ftape + (size_t)a->tape_off[(size_t)a->steps] * a->elem, bytes,
+                                   cudaMemcpyDeviceToDevice, s));
+      a->dt.assign((size_t)a->steps, 0.0);
+      a->iters.assign((size_t)a->steps, 0);
+      if (!rc && a->steps) rc = amx_history(a->plan, a->dt.data(), a->iters.data(), a->steps, stream);
+      if (rc) return rc;
+      if (info) *info = inf;
+      a->taped = (inf.status == 0);
+      a->have_forward = (inf.status == 0);
+      return inf.status ? inf.status : AMX_OK;
+    }
+    // out of room: run again with checkpoints (the caller's state is untouched)
+    rc = amx_plan_reset(a->plan, stream);
+    if (rc) return rc;
+    inf = amx_run_info{};
+  }
   int64_t done = 0;
   for (size_t seg = 0;; ++seg) {
     if (seg >= a->ckpt.size()) {
@@ -206,6 +294,12 @@ int amx_adjoint_forward(amx_adjoint* a, void* state, const amx_params* prm, amx_
   return inf.status ? inf.status : AMX_OK;
 }
 
+int amx_adjoint_uses_stored_tape(const amx_adjoint* a, int32_t* yes) {
+  if (!a || !yes) return AMX_ERR_INVALID_ARG;
+  *yes = a->taped ? 1 : 0;
+  return AMX_OK;
+}
+
 int amx_adjoint_schedule(amx_adjoint* a, double* dt_host, int32_t* iters_host, int64_t n, int64_t* steps) {
   if (!a) return AMX_ERR_INVALID_ARG;
   if (steps) *steps = a->steps;
@@ -225,6 +319,19 @@ int amx_adjoint_backward(amx_adjoint* a, const void* grad_final, void* grad_init
   void *lamA = nullptr, *lamB = nullptr;
   int rc = scratch_view(a, &w, &lamA, &lamB);
   if (rc) return rc;
+  if (a->taped) {
+    std::vector<TapeView> tv;
+    layout_stored(a, &tv);
+    rc = copy_state(a, lamA, grad_final, s);
+    for (int64_t i = (int64_t)tv.size() - 1; i >= 0 && !rc; --i) {
+      rc = a->ops.adjoint(&a->cfg, &a->prm, tv[(size_t)i], lamA, lamB, w, s);
+      std::swap(lamA, lamB);
+    }
+    if (rc) return rc;
+    rc = copy_state(a, grad_initial, lamA, s);
+    rc |= cuda_ok(cudaStreamSynchronize(s));
+    return rc;
+  }
   size_t need = 0;
   const int64_t nseg = (a->steps + a->every - 1) / a->every;
   for (int64_t g = 0; g < nseg; ++g)
@@ -288,7 +395,9 @@ int amx_adjoint_replay(amx_adjoint* a, void* state, void* stream) {
 int amx_adjoint_memory(const amx_adjoint* a, size_t* checkpoint_bytes, size_t* tape_bytes) {
   if (!a) return AMX_ERR_INVALID_ARG;
   if (checkpoint_bytes) *checkpoint_bytes = a->ckpt.size() * (size_t)a->nc * a->elem * a->nvt;
-  if (tape_bytes) *tape_bytes = a->tape_bytes + a->scratch_bytes;
+  // the stored tape counts what the last forward used
+  const size_t stored = a->taped ? (size_t)a->tape_off.back() * a->elem + (size_t)a->nc * a->elem * a->nvt : 0;
+  if (tape_bytes) *tape_bytes = a->tape_bytes + a->scratch_bytes + stored;
   return AMX_OK;
 }
 

@@ -197,84 +197,51 @@ __device__ __forceinline__ long long shifted(const int* ic, int k, int off, int 
   return cell_index<DIM>(j[0], j[1], j[2], n);
 }
 
-// Pointwise part of a hydro stage's adjoint.  P_out = prim(U) (P0 null) or
-// P_out = prim((cons(P0) + cons(prim(U))) / 2).  Writes lU (the cotangent of
-// U = cons(P_in) + flux terms) and sets (or, with `accumulate`, adds)
-// lPin = (d cons(P_in))^T lU; adds the P0 term into lP0.  lPout may alias
-// lPin (each cell reads before it writes).
-template <typename T, int DIM>
-__global__ void __launch_bounds__(kThreads)
-k_stage_point(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lPout, T* lU, T* lPin, T* lP0,
-              int accumulate) {
-  constexpr int NV = DIM + 2;
-  const long long nc = g.nc;
-  const T gamma = T(g.gamma);
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (long long)gridDim.x * blockDim.x) {
-    T q[NV], U[NV], lq[NV], lu[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) { q[v] = Pout[v * nc + c]; lq[v] = lPout[v * nc + c]; }
-    prim_to_cons<T, DIM>(q, U, gamma);
-    cons_to_prim_vjp<T, DIM>(U, lq, gamma, lu);
-    if (P0) {
-      T q0[NV], l0[NV];
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        lu[v] = T(0.5) * lu[v];
-        q0[v] = P0[v * nc + c];
-        l0[v] = T(0);
-      }
-      prim_to_cons_vjp<T, DIM>(q0, lu, gamma, l0);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) lP0[v * nc + c] += l0[v];
-    }
-    T qi[NV], li[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) { qi[v] = Pin[v * nc + c]; li[v] = T(0); }
-    prim_to_cons_vjp<T, DIM>(qi, lu, gamma, li);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      lU[v * nc + c] = lu[v];
-      lPin[v * nc + c] = accumulate ? lPin[v * nc + c] + li[v] : li[v];
-    }
-  }
-}
-
-// Line tiles of the flux adjoint along axis K: L cells along K by W lines
-// along J (the contiguous axis when K is not, else the next-to-last axis).
+// Line tiles of the flux adjoint along axis K: L = 32 cells along K by W = 8
+// lines along J (the contiguous axis when K is not, else the next-to-last
+// axis); the halo of a line costs 3 + 3 cells of 32.
 template <int DIM, int K>
 struct AxisTile {
   static constexpr bool KFAST = (K == DIM - 1);
-  static constexpr int L = KFAST ? 32 : 8;
-  static constexpr int W = KFAST ? 8 : 32;
+  static constexpr int L = 32;
+  static constexpr int W = 8;
   static constexpr int J = KFAST ? DIM - 2 : DIM - 1;
   static constexpr int M = 3 - K - J;  // third axis (3D only)
-  static constexpr int PL = L + 6, UL = L + 4, DL = L + 4, FL = L + 3;
+  static constexpr int PL = L + 6, UL = L + 4, FL = L + 3;
+  // one thread per face and per cell: every phase but the halo load runs in
+  // a single round
+  static constexpr int THREADS = W * (L + 4);
   template <typename T>
   static constexpr size_t smem(int nv) {
-    return sizeof(T) * (size_t)nv * W * (PL + UL + 3 * DL + 2 * FL);
+    return sizeof(T) * (size_t)nv * W * (PL + UL + 2 * FL);
   }
 };
 
-// lPin += the flux terms of one axis: for every face f (between cells f-1
-// and f) of the tile and its reach, the cotangent of the HLL flux
+// The flux terms of one axis: for every face f (between cells f-1 and f) of
+// the tile and its reach, the cotangent of the HLL flux
 // lF = dt/dx (lU[f] - lU[f-1]) is pulled back through the flux and the
 // limited reconstruction qL = P[f-1] + D[f-1], qR = P[f] - D[f],
 // D[m] = minmod((P[m] - P[m-1]) / dx, (P[m+1] - P[m]) / dx) dx / 2
 // (reconstruction.py:399-431, limited_gradients.py:22-88), and every cell of
-// the tile gathers the faces that read it (f in [m-1, m+2]).
-template <typename T, int DIM, int K>
-__global__ void __launch_bounds__(kThreads)
-k_stage_axis(AdjGrid<T> g, const T* Pin, const T* lU, T* lPin, T h) {
+// the tile gathers the faces that read it (f in [m-1, m+2]) into lPin.
+//
+// FIRST (the pass along the contiguous axis, which runs first) also does the
+// pointwise part of the stage: it forms lU from the stage output (P_out =
+// prim(U), or with P0 the RK2 combination prim((cons(P0) + cons(prim(U)))/2),
+// whose cons(prim(.)) is differentiated as the identity) on its line
+// segments, writes lU for the other passes, adds the P0 term into lP0 and
+// sets (or, with `accumulate`, adds) lPin = (d cons(P_in))^T lU + its own
+// flux terms.  The other passes add their flux terms to lPin.
+template <typename T, int DIM, int K, bool FIRST>
+__global__ void __launch_bounds__(AxisTile<DIM, K>::THREADS, sizeof(T) == 4 ? 4 : 2)
+k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lPout, T* lU, T* lPin, T* lP0,
+             int accumulate, T h) {
   using A = AxisTile<DIM, K>;
   constexpr int NV = DIM + 2, L = A::L, W = A::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sP = reinterpret_cast<T*>(smem_raw);   // [NV][W][PL], cell m at m + 3
   T* sU = sP + NV * W * A::PL;              // [NV][W][UL], cell m at m + 2
-  T* sD = sU + NV * W * A::UL;              // [NV][W][DL] slopes, m at m + 2
-  T* sGa = sD + NV * W * A::DL;             // d minmod / d backward difference
-  T* sGb = sGa + NV * W * A::DL;
-  T* sLL = sGb + NV * W * A::DL;            // [NV][W][FL] cotangent of qL, face f at f + 1
+  T* sLL = sU + NV * W * A::UL;             // [NV][W][FL] cotangent of qL, face f at f + 1
   T* sLR = sLL + NV * W * A::FL;
   const int n = g.n;
   const long long nc = g.nc;
@@ -298,51 +265,66 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* lU, T* lPin, T h) {
     if (DIM == 3) ic[A::M] = oM;
     return cell_index<DIM>(ic[0], ic[1], ic[2], n);
   };
+  // element e of a [W][len] array: lines vary fastest when K is not the
+  // contiguous axis (then the lines are contiguous in memory)
+  auto split = [&](int e, int len, int* w, int* m) {
+    if (A::KFAST) { *w = e / len; *m = e % len; } else { *w = e % W; *m = e / W; }
+  };
 
   // loads: P for m in [-3, L+2], lU for m in [-2, L+1]
   for (int e = threadIdx.x; e < W * A::PL; e += blockDim.x) {
-    const int w = e / A::PL, m = e % A::PL - 3;
+    int w, m;
+    split(e, A::PL, &w, &m);
+    m -= 3;
     if (oJ + w >= n) continue;
     const long long c = cell(m, w);
 #pragma unroll
     for (int v = 0; v < NV; ++v) sP[(v * W + w) * A::PL + m + 3] = Pin[v * nc + c];
   }
   for (int e = threadIdx.x; e < W * A::UL; e += blockDim.x) {
-    const int w = e / A::UL, m = e % A::UL - 2;
+    int w, m;
+    split(e, A::UL, &w, &m);
+    m -= 2;
     if (oJ + w >= n) continue;
     const long long c = cell(m, w);
+    T lu[NV];
+    if (FIRST) {
+      T q[NV], U[NV], lq[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) sU[(v * W + w) * A::UL + m + 2] = lU[v * nc + c];
-  }
-  __syncthreads();
-  // slopes and their derivative weights for m in [-2, L+1]
-  for (int e = threadIdx.x; e < W * A::DL; e += blockDim.x) {
-    const int w = e / A::DL, m = e % A::DL - 2;
-    if (oJ + w >= n) continue;
+      for (int v = 0; v < NV; ++v) { q[v] = Pout[v * nc + c]; lq[v] = lPout[v * nc + c]; }
+      prim_to_cons<T, DIM>(q, U, gamma);
+      cons_to_prim_vjp<T, DIM>(U, lq, gamma, lu);
+      if (P0) {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      const T* s = sP + (v * W + w) * A::PL + m + 3;
-      const T bd = (s[0] - s[-1]) / dxT, fd = (s[1] - s[0]) / dxT;
-      T ga, gb;
-      minmod_d(bd, fd, &ga, &gb);
-      const int o = (v * W + w) * A::DL + m + 2;
-      sD[o] = limited(bd, fd, 0, dxT) * dxT / T(2);
-      sGa[o] = ga;
-      sGb[o] = gb;
+        for (int v = 0; v < NV; ++v) lu[v] = T(0.5) * lu[v];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) lu[v] = lU[v * nc + c];
     }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sU[(v * W + w) * A::UL + m + 2] = lu[v];
   }
   __syncthreads();
+  // the limited slope D[m] of the line at cell m and its partial derivatives
+  // (recomputed where needed: cheaper than shared-memory round trips)
+  auto slope = [&](const T* sp, int m, T* ga, T* gb) -> T {
+    const T bd = (sp[m] - sp[m - 1]) / dxT, fd = (sp[m + 1] - sp[m]) / dxT;
+    if (ga) minmod_d(bd, fd, ga, gb);
+    return limited(bd, fd, 0, dxT) * dxT / T(2);
+  };
   // faces f in [-1, L+1]
   for (int e = threadIdx.x; e < W * A::FL; e += blockDim.x) {
-    const int w = e / A::FL, f = e % A::FL - 1;
+    int w, f;
+    split(e, A::FL, &w, &f);
+    f -= 1;
     if (oJ + w >= n) continue;
     T qL[NV], qR[NV], lF[NV], lL[NV], lR[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const T* s = sP + (v * W + w) * A::PL + 3;
-      const T* dd = sD + (v * W + w) * A::DL + 2;
-      qL[v] = s[f - 1] + dd[f - 1];
-      qR[v] = s[f] - dd[f];
+      const T* sp = sP + (v * W + w) * A::PL + 3;
+      qL[v] = sp[f - 1] + slope(sp, f - 1, nullptr, nullptr);
+      qR[v] = sp[f] - slope(sp, f, nullptr, nullptr);
       const T* u = sU + (v * W + w) * A::UL + 2;
       // U[i] += inv_dx (F[i-1/2] - F[i+1/2]) h: face f feeds cell f (+) and f - 1 (-)
       lF[v] = inv_dx * (u[f] - u[f - 1]) * h;
@@ -360,20 +342,45 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* lU, T* lPin, T h) {
   // cells of the tile
   for (int e = threadIdx.x; e < W * L; e += blockDim.x) {
     int w, l;
-    if (A::KFAST) { l = e % L; w = e / L; } else { w = e % W; l = e / W; }
+    split(e, L, &w, &l);
     if (oJ + w >= n || oK + l >= n) continue;
     const long long c = cell(l, w);
+    T r[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       const T* LL = sLL + (v * W + w) * A::FL + 1;
       const T* LR = sLR + (v * W + w) * A::FL + 1;
-      const T* Ga = sGa + (v * W + w) * A::DL + 2;
-      const T* Gb = sGb + (v * W + w) * A::DL + 2;
+      const T* sp = sP + (v * W + w) * A::PL + 3;
+      T ga0, gb0, gap, gbp, gam, gbm;
+      slope(sp, l, &ga0, &gb0);
+      slope(sp, l + 1, &gap, &gbp);
+      slope(sp, l - 1, &gam, &gbm);
       // cotangent of the slope D[m] = lqL[m+1] - lqR[m]
       const T dm1 = LL[l] - LR[l - 1], d0 = LL[l + 1] - LR[l], dp1 = LL[l + 2] - LR[l + 1];
-      const T r = LL[l + 1] + LR[l] + d0 * (Ga[l] - Gb[l]) / T(2) - dp1 * Ga[l + 1] / T(2) +
-                  dm1 * Gb[l - 1] / T(2);
-      lPin[v * nc + c] += r;
+      r[v] = LL[l + 1] + LR[l] + d0 * (ga0 - gb0) / T(2) - dp1 * gap / T(2) + dm1 * gbm / T(2);
+    }
+    if (FIRST) {
+      T lu[NV], qi[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        lu[v] = sU[(v * W + w) * A::UL + l + 2];
+        qi[v] = sP[(v * W + w) * A::PL + l + 3];
+        lU[v * nc + c] = lu[v];
+      }
+      prim_to_cons_vjp<T, DIM>(qi, lu, gamma, r);
+      if (P0) {
+        T q0[NV], l0[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) { q0[v] = P0[v * nc + c]; l0[v] = T(0); }
+        prim_to_cons_vjp<T, DIM>(q0, lu, gamma, l0);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) lP0[v * nc + c] += l0[v];
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v) lPin[v * nc + c] = accumulate ? lPin[v * nc + c] + r[v] : r[v];
+    } else {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) lPin[v * nc + c] += r[v];
     }
   }
 }
@@ -604,7 +611,7 @@ k_tape_mag(FVArgs<T> a, const T* Z, T* Zn, T h) {
   MagSrc<T, DIM> src = Z ? MagSrc<T, DIM>{Z, Z + 3 * nc, false}
                          : MagSrc<T, DIM>{a.state + (DIM + 2) * nc, a.state + nc, true};
   T change = T(0);
-  MagItems<T, DIM>::direct(a, src, Zn, h, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
+  MagItems<T, DIM>::direct(a, a.state, src, Zn, h, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
                            (long long)gridDim.x * blockDim.x, &change);
 }
 
@@ -612,7 +619,7 @@ template <typename T, int DIM>
 __global__ void __launch_bounds__(kFVThreads)
 k_tape_final(FVArgs<T> a, const T* Z) {
   double m[3] = {0.0, 0.0, 0.0};
-  MagItems<T, DIM>::finalize(a, Z, (long long)blockIdx.x * blockDim.x + threadIdx.x, a.ncells,
+  MagItems<T, DIM>::finalize(a, a.state, Z, a.state, (long long)blockIdx.x * blockDim.x + threadIdx.x, a.ncells,
                              (long long)gridDim.x * blockDim.x, false, m);
 }
 
@@ -655,38 +662,40 @@ inline int grid_for(long long nc) {
   return (int)(b < 4096 ? b : 4096);
 }
 
+template <typename T, int DIM, int K, bool FIRST>
+int axis_attr() {
+  return (int)cudaFuncSetAttribute(k_stage_axis<T, DIM, K, FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)AxisTile<DIM, K>::template smem<T>(DIM + 2));
+}
+
 template <typename T, int DIM>
 int set_attrs() {
-  constexpr int NV = DIM + 2;
-  int rc = 0;
-  rc |= (int)cudaFuncSetAttribute(k_stage_axis<T, DIM, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)AxisTile<DIM, 0>::template smem<T>(NV));
-  rc |= (int)cudaFuncSetAttribute(k_stage_axis<T, DIM, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)AxisTile<DIM, 1>::template smem<T>(NV));
-  if (DIM == 3)
-    rc |= (int)cudaFuncSetAttribute(k_stage_axis<T, DIM, DIM - 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)AxisTile<DIM, DIM - 1>::template smem<T>(NV));
+  int rc = axis_attr<T, DIM, DIM - 1, true>();
+  rc |= axis_attr<T, DIM, 0, false>();
+  if (DIM == 3) rc |= axis_attr<T, DIM, 1, false>();
   rc |= (int)cudaFuncSetAttribute(k_tape_stage<T, DIM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)TileGeom<T, DIM>::SMEM);
   return rc ? AMX_ERR_CUDA : AMX_OK;
 }
 
-template <typename T, int DIM, int K>
-void launch_axis(const AdjGrid<T>& g, const T* Pin, const T* lU, T* lPin, T h, cudaStream_t s) {
+template <typename T, int DIM, int K, bool FIRST>
+void launch_axis(const AdjGrid<T>& g, const T* Pin, const T* Pout, const T* P0, const T* lPout, T* lU, T* lPin,
+                 T* lP0, int accumulate, T h, cudaStream_t s) {
   using A = AxisTile<DIM, K>;
   const long long blocks = (long long)((g.n + A::L - 1) / A::L) * ((g.n + A::W - 1) / A::W) * (DIM == 3 ? g.n : 1);
-  k_stage_axis<T, DIM, K><<<(unsigned)blocks, kThreads, A::template smem<T>(DIM + 2), s>>>(g, Pin, lU, lPin, h);
+  k_stage_axis<T, DIM, K, FIRST><<<(unsigned)blocks, A::THREADS, A::template smem<T>(DIM + 2), s>>>(
+      g, Pin, Pout, P0, lPout, lU, lPin, lP0, accumulate, h);
 }
 
 // Reverse of one hydro stage: lPout -> lPin (set, or added with
-// `accumulate`), and the RK2 combination's P0 term into lP0.
+// `accumulate`), and the RK2 combination's P0 term into lP0.  The pass along
+// the contiguous axis goes first (it forms lU and initialises lPin).
 template <typename T, int DIM>
 void stage_adjoint(const AdjGrid<T>& g, const T* Pin, const T* Pout, const T* P0, const T* lPout, T* lU, T* lPin,
                    T* lP0, int accumulate, T h, cudaStream_t s) {
-  k_stage_point<T, DIM><<<grid_for(g.nc), kThreads, 0, s>>>(g, Pin, Pout, P0, lPout, lU, lPin, lP0, accumulate);
-  launch_axis<T, DIM, 0>(g, Pin, lU, lPin, h, s);
-  launch_axis<T, DIM, 1>(g, Pin, lU, lPin, h, s);
-  if (DIM == 3) launch_axis<T, DIM, DIM - 1>(g, Pin, lU, lPin, h, s);
+  launch_axis<T, DIM, DIM - 1, true>(g, Pin, Pout, P0, lPout, lU, lPin, lP0, accumulate, h, s);
+  launch_axis<T, DIM, 0, false>(g, Pin, Pout, P0, lPout, lU, lPin, lP0, accumulate, h, s);
+  if (DIM == 3) launch_axis<T, DIM, 1, false>(g, Pin, Pout, P0, lPout, lU, lPin, lP0, accumulate, h, s);
 }
 
 // Records one step of the forward (dt, k given) into `t`; S0 is filled.

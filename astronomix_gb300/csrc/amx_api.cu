@@ -395,6 +395,54 @@ int amx_run_until(amx_plan* p, void* state, const amx_params* prm, int64_t max_s
   return AMX_OK;
 }
 
+}  // extern "C"
+
+namespace amx {
+
+// Full FV steps in tape mode (fv_kernels.cuh): the start state is at
+// tape + tape_off[steps so far]; every intermediate state of every step is
+// appended to the tape and tape_off records where each step's end state
+// starts.  Stops at t_end, after max_steps, or with AMX_ERR_TOO_LARGE in
+// info->status when the tape is full.  Used by the adjoint's forward pass.
+int fv_run_tape(amx_plan* p, const amx_params* prm, void* tape, long long tape_cap, long long* tape_off,
+                int64_t max_steps, amx_run_info* info, cudaStream_t s) {
+  if (!p || p->fd || !prm || !tape || !tape_off || !info) return AMX_ERR_INVALID_ARG;
+  const int64_t chunk = 1 << 16;
+  int64_t done = 0;
+  amx_run_info tmp{};
+  while (done < max_steps) {
+    const int64_t k = std::min<int64_t>(chunk, max_steps - done);
+    int rc;
+    if (p->cfg.dtype == AMX_F32) {
+      auto a = make_fv_args<float>(p, tape, prm, amx::FV_MODE_STEPS);
+      a.max_steps = k;
+      a.tape = static_cast<float*>(tape);
+      a.tape_cap = tape_cap;
+      a.tape_off = tape_off;
+      rc = fv_launch(p, a, s);
+    } else {
+      auto a = make_fv_args<double>(p, tape, prm, amx::FV_MODE_STEPS);
+      a.max_steps = k;
+      a.tape = static_cast<double*>(tape);
+      a.tape_cap = tape_cap;
+      a.tape_off = tape_off;
+      rc = fv_launch(p, a, s);
+    }
+    if (rc) return rc;
+    rc = read_info(p, &tmp, s);
+    if (rc) return rc;
+    done += k;
+    if (!(tmp.t < prm->t_end)) break;
+    if (tmp.status & (AMX_ERR_TIMEOUT | AMX_ERR_NAN | AMX_ERR_TOO_LARGE)) break;
+  }
+  *info = tmp;
+  return AMX_OK;
+}
+
+}  // namespace amx
+
+extern "C" {
+
 int amx_history(amx_plan* p, double* dt_host, int32_t* iters_host, int64_t n, void* stream) {
   if (!p || n < 0) return AMX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);

@@ -250,7 +250,7 @@ fv_batch_kernel(BatchArgs<T> b) {
       const long long c0 = (long long)(g - s_pref[r]) * kBatchChunk;
       const long long c1 = min(nc, c0 + kBatchChunk);
       const T h = T(s_dt[r]);
-      MagItems<T, DIM>::direct(a, ms, dst, h, c0 + threadIdx.x, c1, blockDim.x, &change);
+      MagItems<T, DIM>::direct(a, a.state, ms, dst, h, c0 + threadIdx.x, c1, blockDim.x, &change);
     }
     if (cur >= 0) {
       const double v = block_max<double>((double)change, red);
@@ -315,7 +315,7 @@ fv_batch_kernel(BatchArgs<T> b) {
       const T* Bv = (s_flag[r] & 4) ? a.mag1 : a.mag0;
       const long long c0 = (long long)(g - s_pref[r]) * kBatchChunk;
       const long long c1 = min(a.ncells, c0 + kBatchChunk);
-      MagItems<T, DIM>::finalize(a, Bv, c0 + threadIdx.x, c1, blockDim.x, track, m);
+      MagItems<T, DIM>::finalize(a, a.state, Bv, a.state, c0 + threadIdx.x, c1, blockDim.x, track, m);
     }
     if (track && cur >= 0) batch_fold<DIM>(m, rc[cur].red[rp % 3], red);
     ++rp;

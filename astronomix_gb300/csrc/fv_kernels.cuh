@@ -82,6 +82,11 @@ struct FVArgs {
   int max_iters;     // fixed-point cap (1000 in the reference)
   long long max_steps;
   double t_pause;    // full-step mode stops before a step that starts at t >= t_pause
+  // Tape mode (full steps): every intermediate state of every step is kept
+  // in `tape` (see the tape layout at fv_run_kernel); null otherwise.
+  T* tape;
+  long long tape_cap;   // elements of `tape`
+  long long* tape_off;  // [max_hist + 1] element offset of each step's start state
 };
 
 // per-item entry points, defined below
@@ -223,11 +228,10 @@ __device__ __forceinline__ void track_maxima(const T* q, T gamma, double* m) {
 // Per-axis maxima of |u_a| + c over all cells of the state (the reference's
 // ghost cells are copies of interior cells and add nothing to the maximum).
 template <typename T, int DIM>
-__device__ __noinline__ void phase_cfl(const FVArgs<T>& a, unsigned long long* slot, double* red) {
+__device__ __noinline__ void phase_cfl(const FVArgs<T>& a, const T* st, unsigned long long* slot, double* red) {
   const T gamma = T(a.gamma);
   double m[3] = {0.0, 0.0, 0.0};
   const long long nc = a.ncells;
-  const T* st = a.state;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
        c += (long long)gridDim.x * blockDim.x) {
     T q[DIM + 2];
@@ -473,8 +477,8 @@ struct MagCtx {
   T dx;
   bool midpoint;
   AxisMap<DIM> amap;
-  __device__ __forceinline__ explicit MagCtx(const FVArgs<T>& a)
-      : state(a.state), nc(a.ncells), n(a.n), dx(T(a.dx)), midpoint(a.integrator == 0), amap(a) {}
+  __device__ __forceinline__ MagCtx(const FVArgs<T>& a, T* st)
+      : state(st), nc(a.ncells), n(a.n), dx(T(a.dx)), midpoint(a.integrator == 0), amap(a) {}
   // the cell `off` cells away along axis k, boundary-mapped
   __device__ __forceinline__ long long neighbor(const int* ic, int k, int off) const {
     int j[3] = {ic[0], ic[1], ic[2]};
@@ -567,11 +571,11 @@ __device__ __forceinline__ void mag_direct_cell(const MagCtx<T, DIM>& x, const M
 // reuse).  Used when the state is L2-resident (2D), where the tiled variant
 // below loses more to tile imbalance and barriers than it saves in loads.
 template <typename T, int DIM>
-__device__ __noinline__ void phase_mag_iterate_direct(const FVArgs<T>& a, MagSrc<T, DIM> src, T* dst, T dt,
-                                  unsigned long long* slot, double* red) {
+__device__ __noinline__ void phase_mag_iterate_direct(const FVArgs<T>& a, T* state, MagSrc<T, DIM> src, T* dst,
+                                                      T dt, unsigned long long* slot, double* red) {
   const long long nc = a.ncells;
   T change = T(0);
-  MagItems<T, DIM>::direct(a, src, dst, dt, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
+  MagItems<T, DIM>::direct(a, state, src, dst, dt, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
                            (long long)gridDim.x * blockDim.x, &change);
   const double r = block_max<double>((double)change, red);
   if (threadIdx.x == 0) atomic_max_nonneg(slot, r);
@@ -605,14 +609,13 @@ __device__ __forceinline__ void load_iter(const T* st, const T* src, long long c
 // computes its cross product once.  Folds max |B_k - B_{k+1}| and
 // max |v_k - v_{k+1}| into `slot`.
 template <typename T, int DIM, int V = 0>
-__device__ __forceinline__ void mag_tile(const FVArgs<T>& a, const int* o, const T* src, T* dst, T dt, T* smem,
-                                         T* change_io) {
+__device__ __forceinline__ void mag_tile(const FVArgs<T>& a, const T* state, const int* o, const T* src, T* dst,
+                                         T dt, T* smem, T* change_io) {
   using G = TileGeom<T, DIM, V>;
   const long long nc = a.ncells;
   const int n = a.n;
   const T dx = T(a.dx);
   const bool midpoint = (a.integrator == 0);
-  const T* state = a.state;
   const AxisMap<DIM> amap(a);
   T* sB = smem;                 // [3][MHALO] averaged B
   T* sE = smem + 3 * G::MHALO;  // [3][MHALO] E = B x v
@@ -690,7 +693,7 @@ __device__ __forceinline__ void mag_tile(const FVArgs<T>& a, const int* o, const
 }
 
 template <typename T, int DIM>
-__device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, const T* src, T* dst, T dt,
+__device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, const T* state, const T* src, T* dst, T dt,
                                                unsigned long long* slot, double* red, T* smem) {
   using G = TileGeom<T, DIM>;
   const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
@@ -698,17 +701,19 @@ __device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, const T* src,
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int o[3];
     tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
-    mag_tile<T, DIM>(a, o, src, dst, dt, smem, &change);
+    mag_tile<T, DIM>(a, state, o, src, dst, dt, smem, &change);
   }
   const double r = block_max<double>((double)change, red);
   if (threadIdx.x == 0) atomic_max_nonneg(slot, r);
 }
 
 // Pressure refresh with gamma = 5/3 and write-back of one cell
-// (_magnetic_field_update.py:208-242); tracks |u_a| + c of the updated gas.
+// (_magnetic_field_update.py:208-242) from `state` into `out` (the same
+// array, or a copy that also receives the density); tracks |u_a| + c of the
+// updated gas.
 template <typename T, int DIM>
-__device__ __forceinline__ void mag_finalize_cell(T* state, long long nc, T gamma, const T* Bv, long long c,
-                                                  bool track, double* m) {
+__device__ __forceinline__ void mag_finalize_cell(const T* state, T* out, long long nc, T gamma, const T* Bv,
+                                                  long long c, bool track, double* m) {
   const T g53 = T(5.0 / 3.0);
   const T rho = state[c];
   const T p = state[(DIM + 1) * nc + c];
@@ -728,13 +733,14 @@ __device__ __forceinline__ void mag_finalize_cell(T* state, long long nc, T gamm
   q[0] = rho;
 #pragma unroll
   for (int i = 0; i < DIM; ++i) {
-    state[(1 + i) * nc + c] = vn[i];
+    out[(1 + i) * nc + c] = vn[i];
     q[1 + i] = vn[i];
   }
-  state[(DIM + 1) * nc + c] = pn;
+  out[(DIM + 1) * nc + c] = pn;
   q[DIM + 1] = pn;
 #pragma unroll
-  for (int i = 0; i < 3; ++i) state[(DIM + 2 + i) * nc + c] = Bn[i];
+  for (int i = 0; i < 3; ++i) out[(DIM + 2 + i) * nc + c] = Bn[i];
+  if (out != state) out[c] = rho;
   if (track) track_maxima<T, DIM>(q, gamma, m);
 }
 
@@ -765,48 +771,48 @@ struct FVItems<double, DIM, RS, V> {
 
 template <typename T, int DIM>
 struct MagItems {
-  static __device__ __forceinline__ void direct(const FVArgs<T>& a, const MagSrc<T, DIM>& src, T* dst, T dt,
-                                                long long c, long long end, long long step, T* change) {
-    const MagCtx<T, DIM> x(a);
+  static __device__ __forceinline__ void direct(const FVArgs<T>& a, T* state, const MagSrc<T, DIM>& src, T* dst,
+                                                T dt, long long c, long long end, long long step, T* change) {
+    const MagCtx<T, DIM> x(a, state);
     T ch = *change;
     for (; c < end; c += step) mag_direct_cell<T, DIM>(x, src, dst, dt, c, ch);
     *change = ch;
   }
-  static __device__ __forceinline__ void finalize(const FVArgs<T>& a, const T* Bv, long long c, long long end,
-                                                  long long step, bool track, double* m) {
-    T* state = a.state;
+  static __device__ __forceinline__ void finalize(const FVArgs<T>& a, const T* state, const T* Bv, T* out,
+                                                  long long c, long long end, long long step, bool track,
+                                                  double* m) {
     const long long nc = a.ncells;
     const T gamma = T(a.gamma);
-    for (; c < end; c += step) mag_finalize_cell<T, DIM>(state, nc, gamma, Bv, c, track, m);
+    for (; c < end; c += step) mag_finalize_cell<T, DIM>(state, out, nc, gamma, Bv, c, track, m);
   }
 };
 template <int DIM>
 struct MagItems<double, DIM> {
-  static __device__ __noinline__ void direct(const FVArgs<double>& a, const MagSrc<double, DIM>& src, double* dst,
-                                             double dt, long long c, long long end, long long step,
+  static __device__ __noinline__ void direct(const FVArgs<double>& a, double* state, const MagSrc<double, DIM>& src,
+                                             double* dst, double dt, long long c, long long end, long long step,
                                              double* change) {
-    const MagCtx<double, DIM> x(a);
+    const MagCtx<double, DIM> x(a, state);
     double ch = *change;
     for (; c < end; c += step) mag_direct_cell<double, DIM>(x, src, dst, dt, c, ch);
     *change = ch;
   }
-  static __device__ __noinline__ void finalize(const FVArgs<double>& a, const double* Bv, long long c,
-                                               long long end, long long step, bool track, double* m) {
-    double* state = a.state;
+  static __device__ __noinline__ void finalize(const FVArgs<double>& a, const double* state, const double* Bv,
+                                               double* out, long long c, long long end, long long step, bool track,
+                                               double* m) {
     const long long nc = a.ncells;
     const double gamma = a.gamma;
-    for (; c < end; c += step) mag_finalize_cell<double, DIM>(state, nc, gamma, Bv, c, track, m);
+    for (; c < end; c += step) mag_finalize_cell<double, DIM>(state, out, nc, gamma, Bv, c, track, m);
   }
 };
 
 // The write-back phase over all cells; folds the maxima of |u_a| + c of the
 // updated gas into `out_slot` when given.
 template <typename T, int DIM>
-__device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* Bv, unsigned long long* out_slot,
-                                                double* red) {
+__device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* state, const T* Bv, T* out,
+                                                unsigned long long* out_slot, double* red) {
   const long long nc = a.ncells;
   double m[3] = {0.0, 0.0, 0.0};
-  MagItems<T, DIM>::finalize(a, Bv, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
+  MagItems<T, DIM>::finalize(a, state, Bv, out, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
                              (long long)gridDim.x * blockDim.x, out_slot != nullptr, m);
   if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
@@ -869,9 +875,9 @@ fv_run_kernel(FVArgs<T> a) {
     unsigned long long* slot = &ctl->mag[mag_pass % 3];
     if (DIM == 2) {
       const MagSrc<T, DIM> first{gas + (DIM + 2) * nc, gas + nc, true};
-      phase_mag_iterate_direct<T, DIM>(a, first, a.mag0, h, slot, red);
+      phase_mag_iterate_direct<T, DIM>(a, gas, first, a.mag0, h, slot, red);
     } else {
-      phase_mag_iterate<T, DIM>(a, nullptr, a.mag0, h, slot, red, smem);
+      phase_mag_iterate<T, DIM>(a, gas, nullptr, a.mag0, h, slot, red, smem);
     }
     if (!grid_sync(bar, status)) return -1;
     double change = bits_to_double(*(volatile unsigned long long*)slot);
@@ -884,9 +890,9 @@ fv_run_kernel(FVArgs<T> a) {
       slot = &ctl->mag[mag_pass % 3];
       if (DIM == 2) {
         const MagSrc<T, DIM> src{cur, cur + 3 * nc, false};
-        phase_mag_iterate_direct<T, DIM>(a, src, nxt, h, slot, red);
+        phase_mag_iterate_direct<T, DIM>(a, gas, src, nxt, h, slot, red);
       } else {
-        phase_mag_iterate<T, DIM>(a, cur, nxt, h, slot, red, smem);
+        phase_mag_iterate<T, DIM>(a, gas, cur, nxt, h, slot, red, smem);
       }
       if (!grid_sync(bar, status)) return -1;
       change = bits_to_double(*(volatile unsigned long long*)slot);
@@ -898,7 +904,7 @@ fv_run_kernel(FVArgs<T> a) {
     if (change > a.tol && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_NOT_CONVERGED);
     if (change != change && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_NAN);
     unsigned long long* out = produce_slot();
-    phase_mag_finalize<T, DIM>(a, cur, RS == RS_LF ? out : nullptr, red);
+    phase_mag_finalize<T, DIM>(a, gas, cur, gas, RS == RS_LF ? out : nullptr, red);
     ++rp;
     if (!grid_sync(bar, status)) return -1;
     return it;
@@ -915,7 +921,7 @@ fv_run_kernel(FVArgs<T> a) {
   };
   auto cfl_phase = [&]() -> bool {
     unsigned long long* slot = produce_slot();
-    phase_cfl<T, DIM>(a, slot, red);
+    phase_cfl<T, DIM>(a, gas, slot, red);
     ++rp;
     return grid_sync(bar, status);
   };
@@ -954,9 +960,46 @@ fv_run_kernel(FVArgs<T> a) {
   }
 
   // ---- full time steps (time_integration.py:386-762)
+  //
+  // Tape mode keeps every intermediate state: the step starting at element
+  // offset `toff` of the tape lays out, in rows of ncells values,
+  //   S0 (NVT rows: the step's start state), S1 (NVG: stage 1),
+  //   MHD: S2 (NVT: stage 2 gas rows, B rows of S0), Z0..Zk (6 rows each:
+  //        the fixed-point iterates), S3 (NVT: after the write-back),
+  //        S4 (NVG: stage 3),
+  //   S5 (NVT: the end state) = the next step's S0,
+  // and tape_off[step + 1] records where S5 starts.  A step that would not
+  // fit stops the run with AMX_ERR_TOO_LARGE.
+  constexpr int NVG = DIM + 2, NVT = DIM + 2 + (MHD ? 3 : 0);
+  const bool taping = a.tape != nullptr;
   const long long step0 = *(volatile long long*)&ctl->steps;
+  long long toff = 0;
+  if (taping) {
+    if (step0 > a.max_hist) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_TOO_LARGE);
+      return;
+    }
+    toff = *(volatile long long*)&a.tape_off[step0];
+  }
+  // copies `rows` rows (all blocks, grid-stride; part of the current phase)
+  auto copy_rows = [&](T* dst, const T* src, int rows) {
+    const long long total = (long long)rows * nc;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x)
+      dst[e] = src[e];
+  };
+  auto too_large = [&]() {
+    if (blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_TOO_LARGE);
+  };
   double t = *(volatile double*)&ctl->t;
-  if (!cfl_phase()) return;  // also orders everyone's read of t before it changes
+  if (taping) {
+    unsigned long long* slot = produce_slot();
+    phase_cfl<T, DIM>(a, a.tape + toff, slot, red);
+    ++rp;
+    if (!grid_sync(bar, status)) return;
+  } else if (!cfl_phase()) {
+    return;  // (the barrier also orders everyone's read of t before it changes)
+  }
   for (long long s = 0; s < a.max_steps; ++s) {
     double dt;
     if (t >= a.t_pause) break;
@@ -969,7 +1012,77 @@ fv_run_kernel(FVArgs<T> a) {
     if (a.exact_end_time) dt = fmin(dt, a.t_end - t);
     const T dtT = T(dt);
     int it = 0;
-    if (MHD) {
+    const long long idx = step0 + s;
+    if (taping) {
+      // one tape step (the layout above)
+      if (idx + 1 > a.max_hist) { too_large(); return; }
+      T* S0 = a.tape + toff;
+      T* S1 = S0 + NVT * nc;
+      if (!MHD) {
+        T* S5 = S1 + NVG * nc;
+        if (toff + (long long)(NVT + NVG + NVT) * nc > a.tape_cap) { too_large(); return; }
+        if (!stage(S0, S1, nullptr, dtT, false)) return;
+        if (!stage(S1, S5, S0, dtT, true)) return;
+        toff = S5 - a.tape;
+      } else {
+        T* S2 = S1 + NVG * nc;
+        T* Z0 = S2 + NVT * nc;
+        // room check for the fixed rows and the iterate j (the tail S3, S4, S5 follows it)
+        auto fits = [&](int j) {
+          return toff + (long long)(NVT + NVG + NVT + 6 * (j + 1) + NVT + NVG + NVT) * nc <= a.tape_cap;
+        };
+        if (!fits(0)) { too_large(); return; }
+        const T h = dtT / T(2);
+        copy_rows(S2 + NVG * nc, S0 + NVG * nc, 3);
+        if (!stage(S0, S1, nullptr, h, false)) return;
+        if (!stage(S1, S2, S0, h, false)) return;
+        // magnetic_update on S2 (_magnetic_field_update.py:37-242), iterates kept
+        unsigned long long* slot = &ctl->mag[mag_pass % 3];
+        if (DIM == 2) {
+          const MagSrc<T, DIM> first{S2 + (DIM + 2) * nc, S2 + nc, true};
+          phase_mag_iterate_direct<T, DIM>(a, S2, first, Z0, dtT, slot, red);
+        } else {
+          phase_mag_iterate<T, DIM>(a, S2, nullptr, Z0, dtT, slot, red, smem);
+        }
+        if (!grid_sync(bar, status)) return;
+        double change = bits_to_double(*(volatile unsigned long long*)slot);
+        if (blockIdx.x == 0 && threadIdx.x == 0) ctl->mag[(mag_pass + 2) % 3] = 0ull;
+        ++mag_pass;
+        int k_it = 0;
+        while (change > a.tol && k_it < a.max_iters) {
+          if (!fits(k_it + 1)) { too_large(); return; }
+          T* cur = Z0 + 6 * (long long)k_it * nc;
+          T* nxt = cur + 6 * nc;
+          slot = &ctl->mag[mag_pass % 3];
+          if (DIM == 2) {
+            const MagSrc<T, DIM> src{cur, cur + 3 * nc, false};
+            phase_mag_iterate_direct<T, DIM>(a, S2, src, nxt, dtT, slot, red);
+          } else {
+            phase_mag_iterate<T, DIM>(a, S2, cur, nxt, dtT, slot, red, smem);
+          }
+          if (!grid_sync(bar, status)) return;
+          change = bits_to_double(*(volatile unsigned long long*)slot);
+          if (blockIdx.x == 0 && threadIdx.x == 0) ctl->mag[(mag_pass + 2) % 3] = 0ull;
+          ++mag_pass;
+          ++k_it;
+        }
+        if (change > a.tol && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_NOT_CONVERGED);
+        if (change != change && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_NAN);
+        T* Zk = Z0 + 6 * (long long)k_it * nc;
+        T* S3 = Zk + 6 * nc;
+        T* S4 = S3 + NVT * nc;
+        T* S5 = S4 + NVG * nc;
+        unsigned long long* out = produce_slot();
+        phase_mag_finalize<T, DIM>(a, S2, Zk, S3, RS == RS_LF ? out : nullptr, red);
+        ++rp;
+        if (!grid_sync(bar, status)) return;
+        copy_rows(S5 + NVG * nc, S3 + NVG * nc, 3);
+        if (!stage(S3, S4, nullptr, h, false)) return;
+        if (!stage(S4, S5, S3, h, true)) return;
+        toff = S5 - a.tape;
+        it = k_it;
+      }
+    } else if (MHD) {
       if (!rk2(dtT / T(2), false)) return;
       it = magnetic(dtT);
       if (it < 0) return;
@@ -984,9 +1097,9 @@ fv_run_kernel(FVArgs<T> a) {
       ctl->steps = step0 + s + 1;
       ctl->mag_iters = it;
       ctl->mag_iters_total += it;
-      const long long idx = step0 + s;
       if (a.dt_hist && idx < a.max_hist) a.dt_hist[idx] = dt;
       if (a.it_hist && idx < a.max_hist) a.it_hist[idx] = it;
+      if (taping) a.tape_off[idx + 1] = toff;
     }
   }
 }

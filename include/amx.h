@@ -277,6 +277,14 @@ int amx_adjoint_backward(amx_adjoint* adj, const void* grad_final, void* grad_in
 /* Advances `state` in place with the recorded schedule (fixed dt and
  * iteration counts): the program the gradient is exact for (synchronises). */
 int amx_adjoint_replay(amx_adjoint* adj, void* state, void* stream);
+/* Device bytes the forward may use to store the whole tape (every
+ * intermediate state of every step, written by the forward kernel itself).
+ * When the run fits, the backward reads the stored tape and recomputes
+ * nothing; otherwise (and with 0, the default) the forward keeps
+ * checkpoints and the backward replays one segment at a time. */
+int amx_adjoint_set_tape_budget(amx_adjoint* adj, size_t bytes);
+/* *yes = 1 when the last forward stored the whole tape. */
+int amx_adjoint_uses_stored_tape(const amx_adjoint* adj, int32_t* yes);
 /* Steps of the last forward, and the first n dt / iteration counts. */
 int amx_adjoint_schedule(amx_adjoint* adj, double* dt_host, int32_t* iters_host, int64_t n, int64_t* steps);
 /* Device bytes held for checkpoints and for the tape and cotangents. */

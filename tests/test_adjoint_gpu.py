@@ -32,10 +32,10 @@ def oracle_grad(cfg, prm, rv, s, w):
     return x.grad.numpy(), out.detach().numpy(), rec
 
 
-def gpu_grad(cfg, prm, rv, s, w, every=20, dtype=np.float64):
+def gpu_grad(cfg, prm, rv, s, w, every=20, dtype=np.float64, tape_budget=0):
     import torch
 
-    integ = AdjointIntegrator(cfg, prm, rv, s.shape, dtype, checkpoint_every=every)
+    integ = AdjointIntegrator(cfg, prm, rv, s.shape, dtype, checkpoint_every=every, tape_budget=tape_budget)
     x = torch.from_numpy(s.astype(dtype)).cuda()
     y = integ.forward(x)
     g = integ.backward(torch.from_numpy(w.astype(dtype)).cuda())
@@ -53,12 +53,14 @@ CASES = [
 ]
 
 
+@pytest.mark.parametrize("tape", ["checkpoints", "stored"])
 @pytest.mark.parametrize("name,kw", CASES, ids=[c[0] for c in CASES])
-def test_fp64_gradient_matches_autograd_of_oracle(cuda, name, kw):
+def test_fp64_gradient_matches_autograd_of_oracle(cuda, name, kw, tape):
     cfg, prm, rv, s = smooth_random(kw["dim"], kw["n"], seed=3, mhd=kw["mhd"], t_end=kw["t_end"])
     w = np.random.default_rng(7).standard_normal(s.shape)
     g_ref, y_ref, rec = oracle_grad(cfg, prm, rv, s, w)
-    g, y, integ = gpu_grad(cfg, prm, rv, s, w, every=2)
+    g, y, integ = gpu_grad(cfg, prm, rv, s, w, every=2, tape_budget=0 if tape == "checkpoints" else 1 << 30)
+    assert integ.stored_tape() == (tape == "stored")
     dts, its = integ.schedule()
     assert len(dts) == rec["steps"] >= 3
     if kw["mhd"]:
@@ -67,11 +69,23 @@ def test_fp64_gradient_matches_autograd_of_oracle(cuda, name, kw):
     assert rel(g, g_ref) < 1e-9, rel(g, g_ref)
 
 
-def test_checkpoint_interval_does_not_change_the_gradient(cuda):
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_checkpoint_interval_and_stored_tape_give_the_same_gradient(cuda, dtype):
+    """Checkpoint intervals 1, 3, 50, the whole tape stored by the forward
+    kernel, and a tape budget too small for the run (which falls back to
+    checkpoints) all give the same gradient and the same final state."""
     cfg, prm, rv, s = smooth_random(2, 12, seed=4, mhd=True, t_end=0.04)
+    if dtype == np.float32:
+        cfg = cfg._replace(numerical_precision=0)
+    s = s.astype(dtype)
     w = np.random.default_rng(1).standard_normal(s.shape)
-    gs = [gpu_grad(cfg, prm, rv, s, w, every=e)[0] for e in (1, 3, 50)]
-    assert np.array_equal(gs[0], gs[1]) and np.array_equal(gs[0], gs[2])
+    runs = [gpu_grad(cfg, prm, rv, s, w, every=e, dtype=dtype) for e in (1, 3, 50)]
+    stored = gpu_grad(cfg, prm, rv, s, w, dtype=dtype, tape_budget=1 << 28)
+    small = gpu_grad(cfg, prm, rv, s, w, every=4, dtype=dtype, tape_budget=s.nbytes * 6)
+    assert stored[2].stored_tape() and not small[2].stored_tape()
+    for g, y, _ in runs[1:] + [stored, small]:
+        assert np.array_equal(g, runs[0][0])
+        assert np.array_equal(y, runs[0][1])
 
 
 def test_fp64_gradient_matches_finite_differences_of_replay(cuda):
