@@ -181,6 +181,7 @@ struct AdjGrid {
   int n;
   long long nc;
   double dx;
+  double inv_dx;  // 1 / dx (computed on the host)
   double gamma;
 };
 
@@ -247,7 +248,7 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
   const long long nc = g.nc;
   const T gamma = T(g.gamma);
   const T dxT = T(g.dx);
-  const T inv_dx = T(1.0 / g.dx);
+  const T inv_dx = T(g.inv_dx);
 
   // tile origin
   const int tK = (n + L - 1) / L, tJ = (n + W - 1) / W;
@@ -596,7 +597,7 @@ k_tape_stage(FVArgs<T> a, const T* Pin, T* Pout, const T* P0, T h) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* smem = reinterpret_cast<T*>(smem_raw);
   const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
-  double m[3] = {0.0, 0.0, 0.0};
+  T m[3] = {T(0), T(0), T(0)};
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int o[3];
     tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
@@ -618,7 +619,7 @@ k_tape_mag(FVArgs<T> a, const T* Z, T* Zn, T h) {
 template <typename T, int DIM>
 __global__ void __launch_bounds__(kFVThreads)
 k_tape_final(FVArgs<T> a, const T* Z) {
-  double m[3] = {0.0, 0.0, 0.0};
+  T m[3] = {T(0), T(0), T(0)};
   MagItems<T, DIM>::finalize(a, a.state, Z, a.state, (long long)blockIdx.x * blockDim.x + threadIdx.x, a.ncells,
                              (long long)gridDim.x * blockDim.x, false, m);
 }

@@ -21,6 +21,7 @@ FVArgs<T> fv_args(const amx_config* c, const amx_params* p) {
   a.integrator = c->fv_magnetic_integrator;
   a.lm = 0;
   a.dx = c->grid_spacing;
+  a.inv_dx = 1.0 / c->grid_spacing;
   a.gamma = p->gamma;
   a.C_cfl = p->C_cfl;
   return a;
@@ -33,6 +34,7 @@ AdjGrid<T> grid(const amx_config* c, const amx_params* p) {
   g.nc = 1;
   for (int k = 0; k < c->dimensionality; ++k) g.nc *= c->num_cells;
   g.dx = c->grid_spacing;
+  g.inv_dx = 1.0 / c->grid_spacing;
   g.gamma = p->gamma;
   return g;
 }

@@ -114,6 +114,7 @@ amx::FVArgs<T> make_fv_args(amx_plan* p, void* state, const amx_params* prm, int
   a.fixed_timestep = c.fixed_timestep;
   a.mode = mode;
   a.dx = c.grid_spacing;
+  a.inv_dx = 1.0 / c.grid_spacing;
   a.gamma = prm->gamma;
   a.C_cfl = prm->C_cfl;
   a.t_end = prm->t_end;

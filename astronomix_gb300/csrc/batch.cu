@@ -289,6 +289,7 @@ int amx_batch_create(const amx_config* tmpl, int32_t num_runs, const int32_t* nu
     d.ncells = nc;
     d.n = num_cells[r];
     d.dx = box_size[r] / num_cells[r];
+    d.inv_dx = 1.0 / d.dx;
     d.t_end = 0.0;
   }
   if (cudaMemcpy(b->d_desc, b->desc.data(), sizeof(BatchRunDesc) * num_runs, cudaMemcpyHostToDevice) !=

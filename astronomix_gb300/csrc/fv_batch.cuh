@@ -35,6 +35,7 @@ struct BatchRunDesc {
   int n;
   int pad;
   double dx;
+  double inv_dx;
   double t_end;
 };
 
@@ -81,6 +82,7 @@ __device__ __forceinline__ FVArgs<T> batch_run_args(const BatchArgs<T>& b, int r
   a.n = d.n;
   a.ncells = d.ncells;
   a.dx = d.dx;
+  a.inv_dx = d.inv_dx;
   a.t_end = d.t_end;
   return a;
 }
@@ -122,8 +124,8 @@ __device__ __forceinline__ void batch_prefix(int* pref, int R, F items_of) {
   __syncthreads();
 }
 
-template <int DIM>
-__device__ __forceinline__ void batch_fold(const double* m, unsigned long long* slot, double* red) {
+template <int DIM, typename T>
+__device__ __forceinline__ void batch_fold(const T* m, unsigned long long* slot, double* red) {
   fold_maxima<DIM>(m, slot, red);
 }
 
@@ -184,13 +186,13 @@ fv_batch_kernel(BatchArgs<T> b) {
     clear_next_red();
     const int total = s_pref[R];
     int cur = -1;
-    double m[3] = {0.0, 0.0, 0.0};
+    T m[3] = {T(0), T(0), T(0)};
     for (int g = blockIdx.x; g < total; g += gridDim.x) {
       const int r = batch_find_run(s_pref, R, g);
       if (r != cur) {
         if (track && cur >= 0) {
           batch_fold<DIM>(m, rc[cur].red[rp % 3], red);
-          m[0] = m[1] = m[2] = 0.0;
+          m[0] = m[1] = m[2] = T(0);
         }
         cur = r;
       }
@@ -300,14 +302,14 @@ fv_batch_kernel(BatchArgs<T> b) {
     batch_prefix(s_pref, R, [&](int r) { return chunk_items(r, 1); });
     const int total = s_pref[R];
     int cur = -1;
-    double m[3] = {0.0, 0.0, 0.0};
+    T m[3] = {T(0), T(0), T(0)};
     const bool track = RS == RS_LF;
     for (int g = blockIdx.x; g < total; g += gridDim.x) {
       const int r = batch_find_run(s_pref, R, g);
       if (r != cur) {
         if (track && cur >= 0) {
           batch_fold<DIM>(m, rc[cur].red[rp % 3], red);
-          m[0] = m[1] = m[2] = 0.0;
+          m[0] = m[1] = m[2] = T(0);
         }
         cur = r;
       }
@@ -332,13 +334,13 @@ fv_batch_kernel(BatchArgs<T> b) {
     batch_prefix(s_pref, R, [&](int r) { return chunk_items(r, 1); });
     const int total = s_pref[R];
     int cur = -1;
-    double m[3] = {0.0, 0.0, 0.0};
+    T m[3] = {T(0), T(0), T(0)};
     for (int g = blockIdx.x; g < total; g += gridDim.x) {
       const int r = batch_find_run(s_pref, R, g);
       if (r != cur) {
         if (cur >= 0) {
           batch_fold<DIM>(m, rc[cur].red[rp % 3], red);
-          m[0] = m[1] = m[2] = 0.0;
+          m[0] = m[1] = m[2] = T(0);
         }
         cur = r;
       }

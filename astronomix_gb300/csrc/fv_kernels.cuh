@@ -72,6 +72,7 @@ struct FVArgs {
   int fixed_timestep;
   int mode;
   double dx;
+  double inv_dx;     // 1 / dx (computed on the host)
   double gamma;
   double C_cfl;
   double t_end;
@@ -209,20 +210,23 @@ struct AxisMap {
 // ------------------------------------------------------------ reductions
 
 // Folds per-thread maxima of |u_a| + c into `slot` (block max + atomicMax).
-template <int DIM>
-__device__ __forceinline__ void fold_maxima(const double* m, unsigned long long* slot, double* red) {
+// The maxima are tracked in the state's precision (a maximum is exact in any
+// precision) and widened to FP64 once per block: GB300's FP64 rate is a small
+// fraction of its FP32 rate.
+template <int DIM, typename T>
+__device__ __forceinline__ void fold_maxima(const T* m, unsigned long long* slot, double* red) {
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
-    const double r = block_max<double>(m[k], red);
+    const double r = block_max<double>((double)m[k], red);
     if (threadIdx.x == 0) atomic_max_nonneg(&slot[k], r);
   }
 }
 
 template <typename T, int DIM>
-__device__ __forceinline__ void track_maxima(const T* q, T gamma, double* m) {
+__device__ __forceinline__ void track_maxima(const T* q, T gamma, T* m) {
   const T cs = sound_speed(q[0], q[DIM + 1], gamma);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) m[k] = nanmax(m[k], (double)(Num<T>::abs_(q[1 + k]) + cs));
+  for (int k = 0; k < DIM; ++k) m[k] = nanmax(m[k], Num<T>::abs_(q[1 + k]) + cs);
 }
 
 // Per-axis maxima of |u_a| + c over all cells of the state (the reference's
@@ -230,7 +234,7 @@ __device__ __forceinline__ void track_maxima(const T* q, T gamma, double* m) {
 template <typename T, int DIM>
 __device__ __noinline__ void phase_cfl(const FVArgs<T>& a, const T* st, unsigned long long* slot, double* red) {
   const T gamma = T(a.gamma);
-  double m[3] = {0.0, 0.0, 0.0};
+  T m[3] = {T(0), T(0), T(0)};
   const long long nc = a.ncells;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
        c += (long long)gridDim.x * blockDim.x) {
@@ -255,14 +259,14 @@ __device__ __noinline__ void phase_cfl(const FVArgs<T>& a, const T* st, unsigned
 // |u_a| + c of P_out are folded into `out_slot`.
 template <typename T, int DIM, int RS, int V = 0>
 __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, const T* __restrict__ Pin, T* Pout,
-                                           const T* P0, T dt, const T* alpha, T* smem, double* m, bool track) {
+                                           const T* P0, T dt, const T* alpha, T* smem, T* m, bool track) {
   using G = TileGeom<T, DIM, V>;
   constexpr int NV = G::NV;
   const int n = a.n;
   const long long nc = a.ncells;
   const T gamma = T(a.gamma);
   const T dxT = T(a.dx);
-  const T inv_dx = T(1.0 / a.dx);
+  const T inv_dx = T(a.inv_dx);
   const int limiter = a.limiter;
   const bool lm = a.lm != 0;
   const AxisMap<DIM> amap(a);
@@ -428,7 +432,7 @@ __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __re
                                                unsigned long long* out_slot, double* red) {
   using G = TileGeom<T, DIM>;
   const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
-  double m[3] = {0.0, 0.0, 0.0};
+  T m[3] = {T(0), T(0), T(0)};
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int o[3];
     tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
@@ -713,7 +717,7 @@ __device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, const T* stat
 // updated gas.
 template <typename T, int DIM>
 __device__ __forceinline__ void mag_finalize_cell(const T* state, T* out, long long nc, T gamma, const T* Bv,
-                                                  long long c, bool track, double* m) {
+                                                  long long c, bool track, T* m) {
   const T g53 = T(5.0 / 3.0);
   const T rho = state[c];
   const T p = state[(DIM + 1) * nc + c];
@@ -756,7 +760,7 @@ __device__ __forceinline__ void mag_finalize_cell(const T* state, T* out, long l
 template <typename T, int DIM, int RS, int V>
 struct FVItems {
   static __device__ __forceinline__ void hydro(const FVArgs<T>& a, const int* o, const T* Pin, T* Pout,
-                                               const T* P0, T dt, const T* alpha, T* smem, double* m, bool track) {
+                                               const T* P0, T dt, const T* alpha, T* smem, T* m, bool track) {
     hydro_tile<T, DIM, RS, V>(a, o, Pin, Pout, P0, dt, alpha, smem, m, track);
   }
 };
@@ -780,7 +784,7 @@ struct MagItems {
   }
   static __device__ __forceinline__ void finalize(const FVArgs<T>& a, const T* state, const T* Bv, T* out,
                                                   long long c, long long end, long long step, bool track,
-                                                  double* m) {
+                                                  T* m) {
     const long long nc = a.ncells;
     const T gamma = T(a.gamma);
     for (; c < end; c += step) mag_finalize_cell<T, DIM>(state, out, nc, gamma, Bv, c, track, m);
@@ -811,7 +815,7 @@ template <typename T, int DIM>
 __device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* state, const T* Bv, T* out,
                                                 unsigned long long* out_slot, double* red) {
   const long long nc = a.ncells;
-  double m[3] = {0.0, 0.0, 0.0};
+  T m[3] = {T(0), T(0), T(0)};
   MagItems<T, DIM>::finalize(a, state, Bv, out, (long long)blockIdx.x * blockDim.x + threadIdx.x, nc,
                              (long long)gridDim.x * blockDim.x, out_slot != nullptr, m);
   if (out_slot) fold_maxima<DIM>(m, out_slot, red);
@@ -819,8 +823,10 @@ __device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* sta
 
 // ------------------------------------------------------------ the kernel
 
+// 3D is bound by HBM latency: its FP32 instantiations are held to three resident
+// blocks per SM (85 registers), 1D and 2D to two (128 registers).
 template <typename T, int DIM, int RS, bool MHD>
-__global__ void __launch_bounds__(kFVThreads)
+__global__ void __launch_bounds__(kFVThreads, (DIM == 3 && sizeof(T) == 4) ? 3 : 2)
 fv_run_kernel(FVArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* smem = reinterpret_cast<T*>(smem_raw);

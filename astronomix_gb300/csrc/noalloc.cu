@@ -109,6 +109,7 @@ int launch(const amx_config* c, void* state, const amx_params* prm, int64_t max_
   a.fixed_timestep = c->fixed_timestep;
   a.mode = amx::FV_MODE_STEPS;
   a.dx = c->grid_spacing;
+  a.inv_dx = 1.0 / c->grid_spacing;
   a.gamma = prm->gamma;
   a.C_cfl = prm->C_cfl;
   a.t_end = prm->t_end;

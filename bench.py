@@ -50,7 +50,52 @@ def parse():
     ap.add_argument("--no-arena", action="store_true", help="skip the 256^3 blast comparison")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-run batched ensemble")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 128^3 adjoint workload")
+    ap.add_argument("--case", default=None, choices=["fd", "ensemble", "adjoint"],
+                    help="run one small case of a secondary workload and exit (for profilers)")
     return ap.parse_args()
+
+
+def run_case(name):
+    """Small, self-contained runs of the secondary workloads for ncu captures:
+    fd: FD WENO-CT blast 128^3 FP32, 2 steps; ensemble: 8 turbulent 2D MHD
+    runs (128^2..512^2, t_end / 8) in one batched launch; adjoint: the 3D
+    density-perturbation problem at 96^3 to t = 0.01, forward and backward
+    with the stored tape (a 4 GB tape budget: the case holds a few GB at
+    most)."""
+    import torch
+    from astronomix_gb300 import _native
+
+    if name == "fd":
+        from astronomix_gb300.time_integration import get_plan
+
+        cfg, prm, rv, s = arena_blast(128, "fd")
+        plan = get_plan(cfg, rv, s.shape, np.float32)
+        dev = torch.from_numpy(s).cuda()
+        st = torch.cuda.current_stream().cuda_stream
+        plan.reset(st)
+        info = plan.run(dev.data_ptr(), _native.make_params(prm), 2, st)
+        print(json.dumps({"case": name, "steps": info.steps, "status": info.status}))
+    elif name == "ensemble":
+        from astronomix_gb300.ensemble import Ensemble, turbulent_ensemble_member
+
+        ms = [turbulent_ensemble_member(seed) for seed in range(8)]
+        prms = [m[1]._replace(t_end=m[1].t_end / 8) for m in ms]
+        ens = Ensemble([m[0] for m in ms], prms, ms[0][2], [m[3].shape for m in ms], np.float32)
+        dev = [torch.from_numpy(m[3]).cuda() for m in ms]
+        ens.run(dev)
+        infos, lock = ens.info()
+        print(json.dumps({"case": name, "lock_steps": lock, "status": max(i.status for i in infos)}))
+    else:
+        from astronomix_gb300.adjoint import AdjointIntegrator, density_perturbation_problem
+
+        cfg, prm, rv, s, target = density_perturbation_problem(96, t_end=0.01)
+        integ = AdjointIntegrator(cfg, prm, rv, s.shape, np.float32, tape_budget=4 << 30)
+        y = integ.forward(torch.from_numpy(s).cuda())
+        L, g = _loss_grad(y, torch.from_numpy(target).cuda().double())
+        grad = integ.backward(g)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": name, "steps": len(integ.schedule()[0]), "stored": integ.stored_tape(),
+                          "finite": bool(torch.isfinite(grad).all())}))
 
 
 def dist_setup(args):
@@ -642,6 +687,9 @@ def run_ours(args, rank, world):
 
 def main():
     args = parse()
+    if args.case:
+        run_case(args.case)
+        return
     rank, world = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, rank, world)
