@@ -136,6 +136,7 @@ SIGNATURES = {
     "amx_adjoint_uses_stored_tape": (_I32, [_P, ctypes.POINTER(_I32)]),
     "amx_adjoint_schedule": (_I32, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I32), _I64, ctypes.POINTER(_I64)]),
     "amx_adjoint_memory": (_I32, [_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
+    "amx_probe_fp32_fma": (_I32, [ctypes.POINTER(_D), _P]),
     "amx_version": (ctypes.c_char_p, []),
 }
 
@@ -378,3 +379,10 @@ class Adjoint:
         a, b = ctypes.c_size_t(), ctypes.c_size_t()
         check(self._L.amx_adjoint_memory(self.handle, ctypes.byref(a), ctypes.byref(b)), "amx_adjoint_memory")
         return {"checkpoint_bytes": a.value, "tape_bytes": b.value}
+
+
+def probe_fp32_fma(stream=0) -> float:
+    """Measured FP32 FMA throughput of the current GPU, TFLOP/s."""
+    t = ctypes.c_double()
+    check(lib().amx_probe_fp32_fma(ctypes.byref(t), _P(stream)), "amx_probe_fp32_fma")
+    return t.value

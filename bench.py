@@ -248,6 +248,48 @@ def time_arena(solver, n=256, steps=3):
             "steps_timed": steps}
 
 
+def fd_precision(n=128, t_end=0.02, flop_per_zu=44e3):
+    """FD WENO-CT on the MHD blast of the FD workload (periodic unit cube,
+    rho = 1, p = 10 inside r < 0.1 and 0.1 outside, B = (1, 1, 0)/sqrt 2,
+    C_cfl 1.5, SSPRK(5,4)) at n^3 to t_end in FP32 and FP64 with the same
+    kernels: s/step of each, their ratio, and the relative L1 density error
+    of FP32 against FP64.  The FD kernel's compute roof is the measured FP32
+    FMA rate; `flop_per_zu` is the estimated arithmetic per zone-update of
+    the scheme (eigensystem once per interface, 7 characteristic fields)."""
+    import torch
+    from _cases import blast_fd
+    from astronomix_gb300 import _native
+    from astronomix_gb300.time_integration import get_plan
+
+    st = torch.cuda.current_stream()
+    out = {"grid": [n, n, n], "t_end": t_end}
+    res = {}
+    for name, dt in (("fp32", np.float32), ("fp64", np.float64)):
+        cfg, prm, rv, s = blast_fd(n=n, dtype=dt, t_end=t_end)
+        s = s.astype(dt)
+        plan = get_plan(cfg, rv, s.shape, dt)
+        p = _native.make_params(prm)
+        dev = torch.from_numpy(s).cuda()
+        plan.reset(st.cuda_stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        info = plan.run(dev.data_ptr(), p, 1 << 40, st.cuda_stream)
+        b.record(st)
+        torch.cuda.synchronize()
+        res[name] = dev[0].double()
+        out[name] = {"steps": info.steps, "s_per_step": a.elapsed_time(b) / 1e3 / max(1, info.steps),
+                     "status": info.status}
+        del dev
+    out["fp32_over_fp64"] = out["fp64"]["s_per_step"] / out["fp32"]["s_per_step"]
+    out["l1_err_vs_fp64"] = float((res["fp32"] - res["fp64"]).abs().sum() / res["fp64"].abs().sum())
+    peak = _native.probe_fp32_fma(st.cuda_stream)
+    zu_s = n ** 3 / out["fp32"]["s_per_step"]
+    out["compute_roof"] = {"fp32_fma_tflops_measured": peak, "flop_per_zone_update_estimate": flop_per_zu,
+                           "achieved_tflops_estimate": zu_s * flop_per_zu / 1e12,
+                           "frac": zu_s * flop_per_zu / 1e12 / peak}
+    return out
+
+
 def time_ensemble(num_runs=64, sequential=True):
     """The batched turbulent ensemble: num_runs 2D MHD runs (seeds 0..num_runs-1,
     grid sizes from {128, 192, 256, 384, 512}^2, t_end in [0.05, 0.2], FV HLLC,
@@ -636,7 +678,8 @@ def run_ours(args, rank, world):
 
     arena = {}
     if not args.no_arena:
-        arena = {"fd_blast_fp32": time_arena("fd"), "fv_lf_blast_fp32": time_arena("fv")}
+        arena = {"fd_blast_fp32": time_arena("fd"), "fv_lf_blast_fp32": time_arena("fv"),
+                 "fd_blast_fp32_vs_fp64": fd_precision()}
     ensemble = None if args.no_ensemble else time_ensemble()
     adjoint = None if args.no_adjoint else time_adjoint()
 

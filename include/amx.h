@@ -290,6 +290,13 @@ int amx_adjoint_schedule(amx_adjoint* adj, double* dt_host, int32_t* iters_host,
 /* Device bytes held for checkpoints and for the tape and cotangents. */
 int amx_adjoint_memory(const amx_adjoint* adj, size_t* checkpoint_bytes, size_t* tape_bytes);
 
+/* ---- measurement ---------------------------------------------------------- */
+
+/* No counterpart in the reference: the FP32 FMA throughput of the current GPU
+ * in TFLOP/s (a timed kernel of independent FMA chains), the compute roof of
+ * the FD WENO kernel.  Synchronises. */
+int amx_probe_fp32_fma(double* tflops, void* stream);
+
 /* Library version string. */
 const char* amx_version(void);
 
