@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(kThreads) k_prep(Bufs<T> b, int stage) {
 
 // ---------------------------------------------------------------- WENO
 
-constexpr int kA = 8;             // cells per tile along the flux axis
+// 7 cells per tile: its 8 x 32 interfaces are one task per thread
+constexpr int kA = 7;             // cells per tile along the flux axis
 constexpr int kL = 32;            // lanes per tile across it
 constexpr int kAH = kA + 6;       // staged cells along the axis (halo 3)
 constexpr int kCellVals = 24;     // U(8) F(8) rho' vx vy vz h (5) cf ca cs (3)
