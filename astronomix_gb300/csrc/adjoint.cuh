@@ -446,64 +446,110 @@ __device__ __forceinline__ void curl_c(T (*Fp)[3], T (*Fm)[3], T dx, T* out) {
 //   lX = -h lv' / rho,  lrho += h lv'.X / rho^2
 //   lBa = va x lE + J x lX (+ curl(lJ) in pass 2), lva = lE x Ba, lJ = lX x Ba
 // and lB0 += lB', lv0 += lv'.  Writes lJ, the partial lBa and lva.
+// Tiles of the point-wise magnetic adjoint: 256 cells, halo 1.
+template <int DIM> struct MagAdjTile;
+template <> struct MagAdjTile<2> {
+  static constexpr int T0 = 16, T1 = 16, T2 = 1;
+};
+template <> struct MagAdjTile<3> {
+  static constexpr int T0 = 4, T1 = 8, T2 = 8;
+};
+
+// The averaged B (Ba) and the cotangent lB' of a halo-1 tile are staged in
+// shared memory; each cell reads its neighbours' values there.
 template <typename T, int DIM>
 __global__ void __launch_bounds__(kThreads)
 k_mag_adj1(AdjGrid<T> g, const T* Z, const T* S, const T* lZn, T h, int midpoint, T* lJ, T* lBa, T* lva,
            T* lB0, T* lv0, T* lrho) {
+  using A = MagAdjTile<DIM>;
+  constexpr int H0 = A::T0 + 2, H1 = A::T1 + 2, H2 = (DIM == 3) ? A::T2 + 2 : 1;
+  constexpr int HALO = H0 * H1 * H2;
+  __shared__ T sB[3][HALO];
+  __shared__ T sL[3][HALO];
   const long long nc = g.nc;
   const int n = g.n;
   const T dx = T(g.dx);
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (long long)gridDim.x * blockDim.x) {
-    int ic[3];
-    decompose<DIM>(c, n, ic);
+  const int n0 = (n + A::T0 - 1) / A::T0, n1 = (n + A::T1 - 1) / A::T1;
+  int b = blockIdx.x;
+  const int o0 = (b % n0) * A::T0;
+  b /= n0;
+  const int o1 = (b % n1) * A::T1;
+  b /= n1;
+  const int o2 = (DIM == 3) ? b * A::T2 : 0;
+  for (int e = threadIdx.x; e < HALO; e += blockDim.x) {
+    const int e2 = e % H2, e1 = (e / H2) % H1, e0 = e / (H2 * H1);
+    const int i0 = ((o0 + e0 - 1) % n + n) % n, i1 = ((o1 + e1 - 1) % n + n) % n;
+    const int i2 = (DIM == 3) ? ((o2 + e2 - 1) % n + n) % n : 0;
+    const long long c = cell_index<DIM>(i0, i1, i2, n);
     T Ba[3], va[3];
     avg_at<T, DIM>(Z, S, c, nc, midpoint != 0, Ba, va);
-    T Bp[3][3], Bm[3][3], Lp[3][3], Lm[3][3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-      for (int i = 0; i < 3; ++i) Bp[k][i] = Bm[k][i] = Lp[k][i] = Lm[k][i] = T(0);
-#pragma unroll
-    for (int k = 0; k < DIM; ++k) {
-      T vv[3];
-      const long long cp = shifted<DIM>(ic, k, +1, n), cm = shifted<DIM>(ic, k, -1, n);
-      avg_at<T, DIM>(Z, S, cp, nc, midpoint != 0, Bp[k], vv);
-      avg_at<T, DIM>(Z, S, cm, nc, midpoint != 0, Bm[k], vv);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) { Lp[k][i] = lZn[i * nc + cp]; Lm[k][i] = lZn[i * nc + cm]; }
-    }
-    T J[3], lE[3];
-    curl_c<T, DIM>(Bp, Bm, dx, J);
-    curl_c<T, DIM>(Lp, Lm, dx, lE);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) lE[i] = -h * lE[i];
-    T X[3];
-    cross3(Ba, J, X);
-    const T rho = S[c];
-    T lX[3], lvn[3];
-    T lr = T(0);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      lvn[i] = lZn[(3 + i) * nc + c];
-      lX[i] = -h * lvn[i] / rho;
-      lr += h * lvn[i] * X[i] / (rho * rho);
-    }
-    T t1[3], t2[3], lvA[3], lJc[3];
-    cross3(va, lE, t1);
-    cross3(J, lX, t2);
-    cross3(lE, Ba, lvA);
-    cross3(lX, Ba, lJc);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      lJ[i * nc + c] = lJc[i];
-      lBa[i * nc + c] = t1[i] + t2[i];
-      lva[i * nc + c] = lvA[i];
-      lB0[i * nc + c] += lZn[i * nc + c];
-      lv0[i * nc + c] += lvn[i];
-    }
-    lrho[c] += lr;
+    for (int i = 0; i < 3; ++i) { sB[i][e] = Ba[i]; sL[i][e] = lZn[i * nc + c]; }
   }
+  __syncthreads();
+  const int cl = threadIdx.x;  // one cell per thread
+  const int c2 = (DIM == 3) ? cl % A::T2 : 0;
+  const int c1 = (DIM == 3) ? (cl / A::T2) % A::T1 : cl % A::T1;
+  const int c0 = (DIM == 3) ? cl / (A::T2 * A::T1) : cl / A::T1;
+  const int g0 = o0 + c0, g1 = o1 + c1, g2 = o2 + c2;
+  if (g0 >= n || g1 >= n || (DIM == 3 && g2 >= n)) return;
+  const long long c = cell_index<DIM>(g0, g1, g2, n);
+  const int hc = ((c0 + 1) * H1 + (c1 + 1)) * H2 + (DIM == 3 ? c2 + 1 : 0);
+  const int st[3] = {H1 * H2, H2, 1};
+  T Bp[3][3], Bm[3][3], Lp[3][3], Lm[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) Bp[k][i] = Bm[k][i] = Lp[k][i] = Lm[k][i] = T(0);
+#pragma unroll
+  for (int k = 0; k < DIM; ++k)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      Bp[k][i] = sB[i][hc + st[k]];
+      Bm[k][i] = sB[i][hc - st[k]];
+      Lp[k][i] = sL[i][hc + st[k]];
+      Lm[k][i] = sL[i][hc - st[k]];
+    }
+  T Ba[3], va[3];
+  avg_at<T, DIM>(Z, S, c, nc, midpoint != 0, Ba, va);
+  T J[3], lE[3];
+  curl_c<T, DIM>(Bp, Bm, dx, J);
+  curl_c<T, DIM>(Lp, Lm, dx, lE);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) lE[i] = -h * lE[i];
+  T X[3];
+  cross3(Ba, J, X);
+  const T rho = S[c];
+  T lX[3], lvn[3];
+  T lr = T(0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    lvn[i] = lZn[(3 + i) * nc + c];
+    lX[i] = -h * lvn[i] / rho;
+    lr += h * lvn[i] * X[i] / (rho * rho);
+  }
+  T t1[3], t2[3], lvA[3], lJc[3];
+  cross3(va, lE, t1);
+  cross3(J, lX, t2);
+  cross3(lE, Ba, lvA);
+  cross3(lX, Ba, lJc);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    lJ[i * nc + c] = lJc[i];
+    lBa[i * nc + c] = t1[i] + t2[i];
+    lva[i * nc + c] = lvA[i];
+    lB0[i * nc + c] += sL[i][hc];
+    lv0[i * nc + c] += lvn[i];
+  }
+  lrho[c] += lr;
+}
+
+template <typename T, int DIM>
+unsigned mag_adj_blocks(int n) {
+  using A = MagAdjTile<DIM>;
+  long long b = (long long)((n + A::T0 - 1) / A::T0) * ((n + A::T1 - 1) / A::T1);
+  if (DIM == 3) b *= (n + A::T2 - 1) / A::T2;
+  return (unsigned)b;
 }
 
 // Pass 2: lBa += curl(lJ); then Ba = (Bk + B0)/2 (or Bk) hands lBa, lva to
@@ -511,7 +557,7 @@ k_mag_adj1(AdjGrid<T> g, const T* Z, const T* S, const T* lZn, T h, int midpoint
 template <typename T, int DIM>
 __global__ void __launch_bounds__(kThreads)
 k_mag_adj2(AdjGrid<T> g, const T* lJ, const T* lBa, const T* lva, int midpoint, int first, T* lZ, T* lB0,
-           T* lv0) {
+           T* lv0, T* lS2) {
   const long long nc = g.nc;
   const int n = g.n;
   const T dx = T(g.dx);
@@ -539,8 +585,11 @@ k_mag_adj2(AdjGrid<T> g, const T* lJ, const T* lBa, const T* lva, int midpoint, 
       const T bk = midpoint ? lb / T(2) : lb, vk = midpoint ? lv / T(2) : lv;
       const T b0 = midpoint ? lb / T(2) : T(0), v0 = midpoint ? lv / T(2) : T(0);
       if (first) {
+        // the last pass: v0 is the gas velocity of S2 (its z row is the
+        // synthesised vz = 0 in 2D)
         lB0[i * nc + c] += bk + b0;
-        lv0[i * nc + c] += vk + v0;
+        const T lv = lv0[i * nc + c] + vk + v0;
+        if (i < DIM) lS2[(1 + i) * nc + c] += lv;
       } else {
         lZ[i * nc + c] = bk;
         lZ[(3 + i) * nc + c] = vk;
@@ -573,18 +622,6 @@ k_final_adj(AdjGrid<T> g, const T* lS3, T* lZ, T* lS2, T* lv0) {
       lZ[(3 + i) * nc + c] = (i < DIM) ? lS3[(1 + i) * nc + c] : T(0);
       lv0[i * nc + c] = T(0);
     }
-  }
-}
-
-// lS2's velocity rows += lv0 (the z row of lv0 is the synthesised vz = 0 in 2D)
-template <typename T, int DIM>
-__global__ void __launch_bounds__(kThreads)
-k_add_v0(AdjGrid<T> g, const T* lv0, T* lS2) {
-  const long long nc = g.nc;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc;
-       c += (long long)gridDim.x * blockDim.x) {
-#pragma unroll
-    for (int i = 0; i < DIM; ++i) lS2[(1 + i) * nc + c] += lv0[i * nc + c];
   }
 }
 
@@ -760,14 +797,14 @@ int adjoint_step(const AdjGrid<T>& g, const StepTape<T>& t, bool mhd, int midpoi
   T* lZn = w.lZ0;
   T* lZp = w.lZ1;
   T* lB0 = w.lS2 + NVG * nc;
+  const unsigned mb = mag_adj_blocks<T, DIM>(g.n);
   for (int j = t.iters; j >= 0; --j) {
     const T* Zin = j ? t.Z + 6 * (j - 1) * nc : nullptr;
-    k_mag_adj1<T, DIM><<<gb, kThreads, 0, s>>>(g, Zin, t.S2, lZn, dtT, midpoint, w.lJ, w.lBa, w.lva, lB0, w.lv0,
+    k_mag_adj1<T, DIM><<<mb, kThreads, 0, s>>>(g, Zin, t.S2, lZn, dtT, midpoint, w.lJ, w.lBa, w.lva, lB0, w.lv0,
                                                w.lS2);
-    k_mag_adj2<T, DIM><<<gb, kThreads, 0, s>>>(g, w.lJ, w.lBa, w.lva, midpoint, j == 0, lZp, lB0, w.lv0);
+    k_mag_adj2<T, DIM><<<gb, kThreads, 0, s>>>(g, w.lJ, w.lBa, w.lva, midpoint, j == 0, lZp, lB0, w.lv0, w.lS2);
     T* tmp = lZn; lZn = lZp; lZp = tmp;
   }
-  k_add_v0<T, DIM><<<gb, kThreads, 0, s>>>(g, w.lv0, w.lS2);
   // first half: S2 = C(S0, L(S1)), S1 = L(S0); B rows of S0 pass to S2
   if (cudaMemsetAsync(lS0, 0, row * NVG, s)) return AMX_ERR_CUDA;
   if (cudaMemcpyAsync(lS0 + NVG * nc, lB0, row * 3, cudaMemcpyDeviceToDevice, s)) return AMX_ERR_CUDA;
