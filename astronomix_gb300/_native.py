@@ -65,6 +65,10 @@ class amx_config(ctypes.Structure):
         ("num_timesteps", ctypes.c_int32),
         ("box_size", ctypes.c_double),
         ("grid_spacing", ctypes.c_double),
+        ("split", ctypes.c_int32),
+        ("first_order_fallback", ctypes.c_int32),
+        ("use_max_adaptive_timestep", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

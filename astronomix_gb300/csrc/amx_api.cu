@@ -59,6 +59,7 @@ int validate(const amx_config* c) {
     const int nv = c->dimensionality + 2 + (c->mhd ? 3 : 0);
     if (c->num_vars != nv) return AMX_ERR_INVALID_ARG;
     if (c->mhd && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
+    if (c->split != 0 && c->split != 1) return AMX_ERR_INVALID_ARG;
     if (c->riemann_solver < AMX_HLL || c->riemann_solver > AMX_LAX_FRIEDRICHS) return AMX_ERR_UNSUPPORTED;
     if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA) return AMX_ERR_UNSUPPORTED;
     if (c->boundary_handling == AMX_GHOST_CELLS) {
@@ -123,6 +124,11 @@ amx::FVArgs<T> make_fv_args(amx_plan* p, void* state, const amx_params* prm, int
   a.dt_scale = 1.0;
   a.tol = (c.numerical_precision == 1) ? 1e-10 : 1e-5;
   a.max_iters = 1000;
+  a.split = c.split;
+  a.first_order = c.first_order_fallback;
+  a.use_dt_max = c.use_max_adaptive_timestep;
+  a.dt_max = prm->dt_max;
+  a.p2 = static_cast<T*>(p->mag0);  // the split sweeps' third buffer (free outside the magnetic update)
   a.max_steps = 0;
   a.t_pause = INFINITY;
   return a;
@@ -225,7 +231,7 @@ int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out) 
   const size_t field = (size_t)p->ncells * p->elem;
   size_t off = 0;
   const size_t o_p1 = off; off = align256(off + nv_gas * field);
-  const size_t o_m0 = off; off = align256(off + (cfg->mhd ? 6 : 0) * field);
+  const size_t o_m0 = off; off = align256(off + (cfg->mhd ? 6 : (cfg->split ? nv_gas : 0)) * field);
   const size_t o_m1 = off; off = align256(off + (cfg->mhd ? 6 : 0) * field);
   const size_t o_ctl = off; off = align256(off + sizeof(FVControl));
   const size_t o_dth = off; off = align256(off + sizeof(double) * (size_t)max_history);

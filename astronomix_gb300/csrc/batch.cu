@@ -85,7 +85,7 @@ int validate_template(const amx_config* c) {
   if (c->riemann_solver != AMX_HLL && c->riemann_solver != AMX_HLLC && c->riemann_solver != AMX_HLLC_LM)
     return AMX_ERR_UNSUPPORTED;
   if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA) return AMX_ERR_UNSUPPORTED;
-  if (c->fixed_timestep) return AMX_ERR_UNSUPPORTED;
+  if (c->fixed_timestep || c->split) return AMX_ERR_UNSUPPORTED;
   if (c->boundary_handling == AMX_GHOST_CELLS) {
     for (int k = 0; k < 2; ++k) {
       for (int side = 0; side < 2; ++side) {

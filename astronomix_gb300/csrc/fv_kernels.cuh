@@ -81,6 +81,11 @@ struct FVArgs {
   double dt_scale;   // seam modes
   double tol;        // fixed-point tolerance
   int max_iters;     // fixed-point cap (1000 in the reference)
+  int split;         // 1: dimensionally split MUSCL-Hancock sweeps instead of SSP-RK2
+  int first_order;   // split: piecewise-constant interface states
+  int use_dt_max;    // split: dt = min(dt, dt_max)
+  double dt_max;
+  T* p2;             // split: third sweep buffer (gas rows)
   long long max_steps;
   double t_pause;    // full-step mode stops before a step that starts at t >= t_pause
   // Tape mode (full steps): every intermediate state of every step is kept
@@ -437,6 +442,149 @@ __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __re
     int o[3];
     tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
     FVItems<T, DIM, RS, 0>::hydro(a, o, Pin, Pout, P0, dt, alpha, smem, m, out_slot != nullptr);
+  }
+  if (out_slot) fold_maxima<DIM>(m, out_slot, red);
+}
+
+// ------------------------------------------------------------ split sweep
+
+// MUSCL-Hancock interface state of cell X (reconstruction.py:40-129,
+// Cartesian): the limited gradient g along the sweep axis (1-based velocity
+// index d), the half-step predictor q - dt/2 A_W g with the reference's A_W
+// (u on the diagonal, A[rho][d] = rho, A[p][1] = rho c^2 -- velocity
+// column 1 whatever the axis, as the reference sets it --, A[d][p] = 1/rho;
+// the products summed in increasing column order), then
+// predictor -/+ (dx/2) g at the cell's left / right interface.
+template <typename T, int DIM>
+__device__ __forceinline__ void muscl_states(const T* qm, const T* q0, const T* qp, int d, T gamma, T dt, T dxT,
+                                             int limiter, T* left, T* right) {
+  constexpr int NV = DIM + 2, P = DIM + 1;
+  T g[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) g[v] = limited((q0[v] - qm[v]) / dxT, (qp[v] - q0[v]) / dxT, limiter, dxT);
+  const T rho = q0[0], u = q0[d];
+  const T c = sound_speed(rho, q0[P], gamma);
+  const T half = dt / T(2), dist = dxT / T(2);
+#pragma unroll
+  for (int b = 0; b < NV; ++b) {
+    T proj;
+    if (b == 0) proj = u * g[0] + rho * g[d];
+    else if (b == d) proj = u * g[d] + (T(1) / rho) * g[P];
+    else if (b == P) proj = (rho * (c * c)) * g[1] + u * g[P];
+    else proj = u * g[b];
+    const T pred = q0[b] - half * proj;
+    left[b] = pred - dist * g[b];
+    right[b] = pred + dist * g[b];
+  }
+}
+
+// One split sweep of a tile along axis k (evolve_state.py:52-160):
+// interface states (MUSCL-Hancock, or piecewise constant with
+// first_order), Riemann fluxes along k, U += (1/dx)(F[i-1/2] - F[i+1/2]) dt.
+// The tile carries a halo of 2 along k only.
+template <typename T, int DIM, int RS>
+__device__ __forceinline__ void sweep_tile(const FVArgs<T>& a, const int* o, int k, const T* __restrict__ Pin,
+                                           T* Pout, T dt, const T* alpha, T* smem, T* m, bool track) {
+  using G = TileGeom<T, DIM>;
+  constexpr int NV = G::NV;
+  const int n = a.n;
+  const long long nc = a.ncells;
+  const T gamma = T(a.gamma);
+  const T dxT = T(a.dx);
+  const T inv_dx = T(a.inv_dx);
+  const int limiter = a.limiter;
+  const bool lm = a.lm != 0;
+  const bool first_order = a.first_order != 0;
+  const AxisMap<DIM> amap(a);
+  const int E0 = G::T0 + 4 * (k == 0), E1 = (DIM >= 2) ? G::T1 + 4 * (k == 1) : 1,
+            E2 = (DIM >= 3) ? G::T2 + 4 * (k == 2) : 1;
+  const int HL = E0 * E1 * E2;
+  const int F0 = G::T0 + (k == 0), F1 = (DIM >= 2) ? G::T1 + (k == 1) : 1, F2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
+  const int NF = F0 * F1 * F2;
+  const int stride = (k == 0) ? E1 * E2 : ((k == 1) ? E2 : 1);
+  T* sP = smem;            // [NV][HL]
+  T* sF = smem + NV * HL;  // [NV][NF]
+  for (int e = threadIdx.x; e < HL; e += blockDim.x) {
+    const int e2 = e % E2, e1 = (e / E2) % E1, e0 = e / (E2 * E1);
+    bool f0 = false, f1 = false, f2 = false;
+    const int i0 = amap(0, o[0] + e0 - 2 * (k == 0), &f0);
+    const int i1 = (DIM >= 2) ? amap(1, o[1] + e1 - 2 * (k == 1), &f1) : 0;
+    const int i2 = (DIM >= 3) ? amap(2, o[2] + e2 - 2 * (k == 2), &f2) : 0;
+    const long long c = cell_index<DIM>(i0, i1, i2, n);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      T val = Pin[v * nc + c];
+      if ((v == 1 && f0) || (v == 2 && f1) || (v == 3 && f2)) val = -val;
+      sP[v * HL + e] = val;
+    }
+  }
+  __syncthreads();
+  for (int f = threadIdx.x; f < NF; f += blockDim.x) {
+    const int f2 = f % F2, f1 = (f / F2) % F1, f0 = f / (F2 * F1);
+    // halo index of the cell right of the face
+    const int hr = ((f0 + 2 * (k == 0)) * E1 + (DIM >= 2 ? f1 + 2 * (k == 1) : 0)) * E2 +
+                   (DIM >= 3 ? f2 + 2 * (k == 2) : 0);
+    const int hl = hr - stride;
+    T qL[NV], qR[NV];
+    if (first_order) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) { qL[v] = sP[v * HL + hl]; qR[v] = sP[v * HL + hr]; }
+    } else {
+      T lm1[NV], l0[NV], lp1[NV], rp1[NV], lo[NV], hi[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        lm1[v] = sP[v * HL + hl - stride];
+        l0[v] = sP[v * HL + hl];
+        lp1[v] = sP[v * HL + hr];
+        rp1[v] = sP[v * HL + hr + stride];
+      }
+      muscl_states<T, DIM>(lm1, l0, lp1, k + 1, gamma, dt, dxT, limiter, lo, hi);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) qL[v] = hi[v];  // right extrapolation of the left cell
+      muscl_states<T, DIM>(l0, lp1, rp1, k + 1, gamma, dt, dxT, limiter, lo, hi);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) qR[v] = lo[v];  // left extrapolation of the right cell
+    }
+    T F[NV];
+    riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), lm, F);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sF[v * NF + f] = F[v];
+  }
+  __syncthreads();
+  const int fstride = (k == 0) ? F1 * F2 : ((k == 1) ? F2 : 1);
+  for (int cl = threadIdx.x; cl < G::CELLS; cl += blockDim.x) {
+    const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
+    const int g0 = o[0] + c0, g1 = o[1] + c1, g2 = o[2] + c2;
+    if (!(g0 < n && (DIM < 2 || g1 < n) && (DIM < 3 || g2 < n))) continue;
+    const int h = ((c0 + 2 * (k == 0)) * E1 + (DIM >= 2 ? c1 + 2 * (k == 1) : 0)) * E2 +
+                  (DIM >= 3 ? c2 + 2 * (k == 2) : 0);
+    const int fl = (c0 * F1 + (DIM >= 2 ? c1 : 0)) * F2 + (DIM >= 3 ? c2 : 0);  // face i-1/2
+    const int fr = fl + fstride;
+    T q[NV], U[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) q[v] = sP[v * HL + h];
+    prim_to_cons<T, DIM>(q, U, gamma);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) U[v] = U[v] + inv_dx * (sF[v * NF + fl] - sF[v * NF + fr]) * dt;
+    cons_to_prim<T, DIM>(U, q, gamma);
+    const long long c = cell_index<DIM>(g0, g1, g2, n);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) Pout[v * nc + c] = q[v];
+    if (track) track_maxima<T, DIM>(q, gamma, m);
+  }
+  __syncthreads();  // the next tile overwrites the shared arrays
+}
+
+template <typename T, int DIM, int RS>
+__device__ __noinline__ void phase_sweep(const FVArgs<T>& a, int k, const T* __restrict__ Pin, T* Pout, T dt,
+                                         const T* alpha, T* smem, unsigned long long* out_slot, double* red) {
+  using G = TileGeom<T, DIM>;
+  const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
+  T m[3] = {T(0), T(0), T(0)};
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int o[3];
+    tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
+    sweep_tile<T, DIM, RS>(a, o, k, Pin, Pout, dt, alpha, smem, m, out_slot != nullptr);
   }
   if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
@@ -836,6 +984,7 @@ fv_run_kernel(FVArgs<T> a) {
   const GridBarrier bar{&ctl->bar_count, &ctl->bar_gen, &ctl->abort_flag};
   const long long nc = a.ncells;
   T* gas = a.state;
+  constexpr int NVG_ = DIM + 2;
   __shared__ T s_alpha[3];
 
   // Producer ring of maxima: the phase with pass number rp writes slot rp % 3
@@ -871,10 +1020,46 @@ fv_run_kernel(FVArgs<T> a) {
   };
   // one RK2 update of the gas rows with stage dt `h` (evolve_state.py:419-488);
   // `last`: the update ends the time step
-  auto rk2 = [&](T h, bool last) -> bool {
+  auto rk2_unsplit = [&](T h, bool last) -> bool {
     if (!stage(gas, a.p1, nullptr, h, false)) return false;
     return stage(a.p1, gas, gas, h, last);
   };
+  // one split sweep along axis k (evolve_state.py:52-160)
+  auto sweep = [&](const T* in, T* out, int k, T h, bool need) -> bool {
+    set_alpha();
+    unsigned long long* slot = produce_slot();
+    phase_sweep<T, DIM, RS>(a, k, in, out, h, RS == RS_LF ? s_alpha : nullptr, smem,
+                            (need || RS == RS_LF) ? slot : nullptr, red);
+    ++rp;
+    return grid_sync(bar, status);
+  };
+  // _evolve_gas_state_split (evolve_state.py:168-325): Strang sequence of
+  // sweeps x(h/2) y(h) x(h/2) in 2D, x(h/2) y(h/2) z(h) y(h/2) x(h/2) in 3D,
+  // rotating through the state, p1 and p2 so that the last one lands in the
+  // state; in 1D the single sweep's result is copied back
+  auto split_update = [&](T h, bool last) -> bool {
+    if (DIM == 1) {
+      if (!sweep(gas, a.p1, 0, h, last)) return false;
+      const long long total = (long long)NVG_ * nc;
+      for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+           e += (long long)gridDim.x * blockDim.x)
+        gas[e] = a.p1[e];
+      return grid_sync(bar, status);
+    }
+    const T h2 = h / T(2);
+    if (DIM == 2) {
+      if (!sweep(gas, a.p1, 0, h2, false)) return false;
+      if (!sweep(a.p1, a.p2, 1, h, false)) return false;
+      return sweep(a.p2, gas, 0, h2, last);
+    }
+    if (!sweep(gas, a.p1, 0, h2, false)) return false;
+    if (!sweep(a.p1, a.p2, 1, h2, false)) return false;
+    if (!sweep(a.p2, a.p1, 2, h, false)) return false;
+    if (!sweep(a.p1, a.p2, 1, h2, false)) return false;
+    return sweep(a.p2, gas, 0, h2, last);
+  };
+  // the gas update of the configured scheme
+  auto rk2 = [&](T h, bool last) -> bool { return a.split ? split_update(h, last) : rk2_unsplit(h, last); };
 
   // magnetic_update (_magnetic_field_update.py:37-242); returns iterations or -1
   auto magnetic = [&](T h) -> int {
@@ -917,9 +1102,19 @@ fv_run_kernel(FVArgs<T> a) {
   };
 
   // CFL dt from the maxima of the last producer (_timestep_estimator.py:118-128)
+  // (split: _timestep_estimator.py:130-218, the largest |u_a| + c over all
+  // axes, dt = C dx / w, clamped to dt_max when use_max_adaptive_timestep)
   auto dt_from_maxima = [&]() -> double {
     double m[3];
     last_maxima(m);
+    if (a.split) {
+      double w = m[0];
+#pragma unroll
+      for (int k = 1; k < DIM; ++k) w = nanmax(w, m[k]);
+      double dt = a.C_cfl * a.dx / w;
+      if (a.use_dt_max && dt == dt) dt = fmin(dt, a.dt_max);
+      return dt;
+    }
     double sum = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) sum = (k == 0) ? m[k] / a.dx : sum + m[k] / a.dx;

@@ -68,6 +68,7 @@ int check_config(const amx_config* c) {
   if (c->dimensionality < 1 || c->dimensionality > 3 || c->num_cells < 4) return AMX_ERR_INVALID_ARG;
   if (c->num_vars != c->dimensionality + 2 + (c->mhd ? 3 : 0)) return AMX_ERR_INVALID_ARG;
   if (c->mhd && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
+  if (c->split != 0 && c->split != 1) return AMX_ERR_INVALID_ARG;
   if (c->riemann_solver < AMX_HLL || c->riemann_solver > AMX_LAX_FRIEDRICHS) return AMX_ERR_UNSUPPORTED;
   if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA) return AMX_ERR_UNSUPPORTED;
   if (!(c->grid_spacing > 0.0)) return AMX_ERR_INVALID_ARG;
@@ -117,6 +118,11 @@ int launch(const amx_config* c, void* state, const amx_params* prm, int64_t max_
   a.dt_in = 0.0;
   a.dt_scale = 1.0;
   a.tol = (c->numerical_precision == 1) ? 1e-10 : 1e-5;
+  a.split = c->split;
+  a.first_order = c->first_order_fallback;
+  a.use_dt_max = c->use_max_adaptive_timestep;
+  a.dt_max = prm->dt_max;
+  a.p2 = a.mag0;
   a.max_iters = 1000;
   a.t_pause = INFINITY;
   const int64_t chunk = int64_t(1) << 16;
@@ -147,7 +153,7 @@ extern "C" int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_
   const size_t field = (size_t)nc * elem;
   const size_t o_p1 = align256(sizeof(amx::FVControl));
   const size_t o_m0 = align256(o_p1 + (cfg->dimensionality + 2) * field);
-  const size_t o_m1 = align256(o_m0 + (cfg->mhd ? 6 : 0) * field);
+  const size_t o_m1 = align256(o_m0 + (cfg->mhd ? 6 : (cfg->split ? cfg->dimensionality + 2 : 0)) * field);
   const size_t need = align256(o_m1 + (cfg->mhd ? 6 : 0) * field);
   if (need > kNoallocScratchBytes) return AMX_ERR_TOO_LARGE;
 

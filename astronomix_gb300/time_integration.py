@@ -16,7 +16,7 @@ import numpy as np
 from . import _native
 from .option_classes import (
     FINITE_VOLUME, FINITE_DIFFERENCE, GHOST_CELLS, PERIODIC_ROLL, PERIODIC_BOUNDARY, OPEN_BOUNDARY,
-    UNSPLIT, RK2_SSP, CARTESIAN, SimulationConfig, SimulationParams, BoundarySettings1D,
+    UNSPLIT, SPLIT, RK2_SSP, MUSCL, CARTESIAN, SimulationConfig, SimulationParams, BoundarySettings1D,
 )
 from .variable_registry import RegisteredVariables
 
@@ -54,10 +54,15 @@ def _check_supported(config: SimulationConfig):
             config.turbulent_forcing_config.turbulent_forcing:
         raise NotImplementedError("physics modules are not part of the accelerated MHD step")
     if config.solver_mode == FINITE_VOLUME:
-        if config.split != UNSPLIT:
-            raise NotImplementedError("the split (MUSCL-Hancock) FV scheme is not part of the accelerated path")
-        if config.time_integrator != RK2_SSP:
-            raise ValueError("Only the RK2 SSP time integrator is currently supported for the unsplit scheme.")
+        if config.split == UNSPLIT:
+            if config.time_integrator != RK2_SSP:
+                raise ValueError("Only the RK2 SSP time integrator is currently supported for the unsplit scheme.")
+        elif config.split == SPLIT:
+            if config.time_integrator != MUSCL and not config.first_order_fallback:
+                raise ValueError("Time integrator %d not supported for split reconstruction. Only MUSCL is "
+                                 "supported." % config.time_integrator)
+        else:
+            raise ValueError("unknown split mode %d" % config.split)
     if config.use_specific_snapshot_timepoints:
         raise NotImplementedError("specific snapshot time points are not supported yet")
 
@@ -101,6 +106,9 @@ def make_amx_config(config: SimulationConfig, rv: RegisteredVariables, shape, dt
     c.num_timesteps = int(config.num_timesteps)
     c.box_size = float(config.box_size)
     c.grid_spacing = float(config.grid_spacing)
+    c.split = int(config.split)
+    c.first_order_fallback = int(bool(config.first_order_fallback))
+    c.use_max_adaptive_timestep = int(bool(config.use_max_adaptive_timestep))
     return c
 
 

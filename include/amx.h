@@ -88,6 +88,10 @@ typedef struct amx_config {
   int32_t num_timesteps;
   double box_size;
   double grid_spacing;            /* box_size / num_cells                       */
+  int32_t split;                  /* FV: 0 unsplit (SSP-RK2), 1 split (MUSCL-Hancock sweeps) */
+  int32_t first_order_fallback;   /* split: piecewise-constant interface states */
+  int32_t use_max_adaptive_timestep; /* split: dt = min(dt, dt_max)            */
+  int32_t reserved;
 } amx_config;
 
 /* Traced parameters (astronomix/option_classes/simulation_params.py:11-66). */

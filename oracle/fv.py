@@ -14,7 +14,7 @@ reference's ``axis`` argument) is array axis ``a``.
 from astronomix_gb300.option_classes import (
     GHOST_CELLS, OPEN_BOUNDARY, REFLECTIVE_BOUNDARY, PERIODIC_BOUNDARY,
     MINMOD, OSHER, DOUBLE_MINMOD, SUPERBEE, VAN_ALBADA,
-    HLL, HLLC, HLLC_LM, LAX_FRIEDRICHS, UNSPLIT, RK2_SSP,
+    HLL, HLLC, HLLC_LM, LAX_FRIEDRICHS, UNSPLIT, RK2_SSP, MUSCL,
     IMPLICIT_MIDPOINT, IMPLICIT_EULER, SINGLE_PRECISION, DOUBLE_PRECISION,
 )
 from ._xp import xp
@@ -299,6 +299,43 @@ def reconstruct_unsplit_single(P, config, axis):
     return xp.roll(right_center, 1, axis), left_center
 
 
+def reconstruct_split(P, dt, gamma, config, rv, axis):
+    """reconstruction.py:40-129 (Cartesian): limited gradients, the MUSCL-Hancock
+    half-step predictor P - dt/2 A_W g with the reference's A_W (u on the
+    diagonal, A[rho, axis] = rho, A[p, 1] = rho c^2 -- column 1 whatever the
+    axis, as the reference sets it -- and A[axis, p] = 1 / rho; the einsum's
+    sum over a taken in increasing a), and the interface states."""
+    if config.time_integrator != MUSCL:
+        raise ValueError("Time integrator %d not supported for split reconstruction. Only MUSCL is supported."
+                         % config.time_integrator)
+    rho = P[rv.density_index]
+    p = P[rv.pressure_index]
+    u = P[axis]
+    g = limited_gradients(P, config, axis)
+    c = speed_of_sound(rho, p, gamma)
+    nv = P.shape[0]
+    pi = rv.pressure_index
+    proj = xp.zeros_like(P)
+    for b in range(nv):
+        coef = {b: u}
+        if b == rv.density_index:
+            coef[axis] = rho
+        if b == pi:
+            coef[1] = rho * c ** 2
+        if b == axis:
+            coef[pi] = 1 / rho
+        acc = None
+        for a_ in sorted(coef):
+            term = coef[a_] * g[a_]
+            acc = term if acc is None else acc + term
+        proj[b] = acc
+    predictors = P - dt / 2 * proj
+    dist = config.grid_spacing / 2
+    left = predictors - dist * g
+    right = predictors + dist * g
+    return xp.roll(right, 1, axis), left
+
+
 # ------------------------------------------------------ Riemann solvers
 
 def hll(PL, PR, gamma, dims, rv, d):
@@ -420,6 +457,47 @@ def evolve_gas_unsplit(P, dt, gamma, config, rv):
     U2 = conserved_state_from_primitive(P2, gamma, dims, rv)
     U = 0.5 * (U0 + U2)
     return primitive_state_from_conserved(U, gamma, dims, rv)
+
+
+def evolve_along_axis(P, dt, gamma, config, rv, axis):
+    """evolve_state.py:52-160 (Cartesian): one split sweep along `axis`."""
+    dims = config.dimensionality
+    ghost = config.boundary_handling == GHOST_CELLS
+    if ghost:
+        P = boundary_handler(P, config)
+    U = conserved_state_from_primitive(P, gamma, dims, rv)
+    if config.first_order_fallback:
+        PL, PR = xp.roll(P, 1, axis), P
+    else:
+        PL, PR = reconstruct_split(P, dt, gamma, config, rv, axis)
+    F = riemann_solver(PL, PR, P, gamma, config, rv, axis)
+    U = U + 1 / config.grid_spacing * (F - xp.roll(F, -1, axis)) * dt
+    P = primitive_state_from_conserved(U, gamma, dims, rv)
+    if ghost:
+        P = boundary_handler(P, config)
+    return P
+
+
+def evolve_gas_split(P, dt, gamma, config, rv):
+    """evolve_state.py:168-325: Strang splitting of the axis sweeps."""
+    dims = config.dimensionality
+    if dims == 1:
+        return evolve_along_axis(P, dt, gamma, config, rv, 1)
+    if dims == 2:
+        P = evolve_along_axis(P, dt / 2, gamma, config, rv, 1)
+        P = evolve_along_axis(P, dt, gamma, config, rv, 2)
+        return evolve_along_axis(P, dt / 2, gamma, config, rv, 1)
+    P = evolve_along_axis(P, dt / 2, gamma, config, rv, 1)
+    P = evolve_along_axis(P, dt / 2, gamma, config, rv, 2)
+    P = evolve_along_axis(P, dt, gamma, config, rv, 3)
+    P = evolve_along_axis(P, dt / 2, gamma, config, rv, 2)
+    return evolve_along_axis(P, dt / 2, gamma, config, rv, 1)
+
+
+def evolve_gas(P, dt, gamma, config, rv):
+    if config.split == UNSPLIT:
+        return evolve_gas_unsplit(P, dt, gamma, config, rv)
+    return evolve_gas_split(P, dt, gamma, config, rv)
 
 
 # ----------------------------------------------- magnetic sub-step (Pang-Wu)
@@ -554,21 +632,19 @@ def magnetic_update(B, gas, dx, dt, config, rv, return_iterations=False):
 
 
 def evolve_state_fv(P, dt, gamma, config, rv, stats=None):
-    """evolve_state.py:497-600 (unsplit scheme; MHD via the Pang-Wu split)."""
-    if config.split != UNSPLIT:
-        raise NotImplementedError("the split (MUSCL-Hancock) scheme is not part of the accelerated path")
+    """evolve_state.py:497-600 (unsplit or split gas scheme; MHD via the Pang-Wu split)."""
     if not config.mhd:
-        return evolve_gas_unsplit(P, dt, gamma, config, rv)
+        return evolve_gas(P, dt, gamma, config, rv)
     if config.dimensionality < 2:
         raise ValueError("MHD currently not supported in 1D.")
     rv_gas = rv._replace(num_vars=rv.num_vars - 3)
     gas = P[:-3]
     B = P[-3:]
-    gas = evolve_gas_unsplit(gas, dt / 2, gamma, config, rv_gas)
+    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas)
     B, gas, it = magnetic_update(B, gas, config.grid_spacing, dt, config, rv, return_iterations=True)
     if stats is not None:
         stats.append(it)
-    gas = evolve_gas_unsplit(gas, dt / 2, gamma, config, rv_gas)
+    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas)
     return xp.concatenate([gas, B], axis=0)
 
 
@@ -586,4 +662,21 @@ def cfl_time_step(P, dx, dt_max, gamma, config, rv, C_cfl):
             a = xp.amax(xp.abs(P[axis]) + c) / dx
             total = a if total is None else total + a
         return C_cfl * 1 / total
-    raise NotImplementedError("the split CFL estimate is not part of the accelerated path")
+    # split: wave speeds |u| + c of the cells on either side of every
+    # interface along every axis (get_wave_speeds, :40-88), maximum over axes
+    c = speed_of_sound(rho, p, gamma)
+    w = xp.abs(P[1:dims + 1]) + c
+    nd = P.ndim - 1
+    best = None
+    for axis in range(1, dims + 1):
+        lo = [slice(None)] * nd
+        hi = [slice(None)] * nd
+        lo[axis - 1] = slice(None, -1)
+        hi[axis - 1] = slice(1, None)
+        wa = w[axis - 1]
+        m = xp.maximum(xp.amax(xp.abs(wa[tuple(lo)])), xp.amax(xp.abs(wa[tuple(hi)])))
+        best = m if best is None else xp.maximum(best, m)
+    dt = C_cfl * dx / best
+    if config.use_max_adaptive_timestep:
+        dt = xp.minimum(dt, xp.scalar(dt_max, dt) if hasattr(dt, "dtype") else dt_max)
+    return dt
