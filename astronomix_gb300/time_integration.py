@@ -63,8 +63,6 @@ def _check_supported(config: SimulationConfig):
                                  "supported." % config.time_integrator)
         else:
             raise ValueError("unknown split mode %d" % config.split)
-    if config.use_specific_snapshot_timepoints:
-        raise NotImplementedError("specific snapshot time points are not supported yet")
 
 
 def _bc_codes(config: SimulationConfig):
@@ -101,7 +99,10 @@ def make_amx_config(config: SimulationConfig, rv: RegisteredVariables, shape, dt
         c.bc_lo[k] = int(lo[k])
         c.bc_hi[k] = int(hi[k])
     c.enforce_positivity = int(bool(config.enforce_positivity))
-    c.exact_end_time = int(bool(config.exact_end_time))
+    # with specific snapshot time points, dt is clipped to the next time point
+    # (time_integration.py:671-678): the driver passes that point as t_end
+    c.exact_end_time = int(bool(config.exact_end_time) or
+                           bool(config.use_specific_snapshot_timepoints and config.return_snapshots))
     c.fixed_timestep = int(bool(config.fixed_timestep))
     c.num_timesteps = int(config.num_timesteps)
     c.box_size = float(config.box_size)
@@ -186,39 +187,74 @@ def time_integration(primitive_state, config: SimulationConfig, params: Simulati
         out = restore(dev)
         return StateStruct(primitive_state=out) if config.state_struct else out
 
-    # ---- snapshots: pause before the first step starting at t >= k t_end / n
+    # ---- snapshots
     n = int(config.num_snapshots)
     ss = config.snapshot_settings
-    times, states, mass, energy, internal, kinetic, divb = [], [], [], [], [], [], []
-    k = 0
-    steps_taken = 0
-    while True:
-        thr = k * params.t_end / n if k < n else math.inf
-        info = plan.run_until(ptr, prm, max_steps - steps_taken, thr, stream)
-        _raise_status(info.status, config)
-        steps_taken = info.steps
-        done = (steps_taken >= max_steps) or (not config.fixed_timestep and not (info.t < params.t_end))
-        if done:
-            break
-        # at the start of a step with t >= threshold k
+    rec = {"times": [], "states": [], "mass": [], "energy": [], "internal": [], "kinetic": [], "divb": [],
+           "radial": []}
+
+    def take(t):
         if config.return_snapshots:
-            times.append(info.t)
+            if len(rec["times"]) >= n:
+                return
+            rec["times"].append(t)
             if ss.return_states:
-                states.append(restore(dev.clone()))
+                rec["states"].append(restore(dev.clone()))
             sums = plan.conservation_sums(ptr, prm, stream)
-            mass.append(sums[0])
-            energy.append(sums[1])
-            kinetic.append(sums[2])
-            internal.append(sums[3])
-            divb.append(sums[4])
+            rec["mass"].append(sums[0])
+            rec["energy"].append(sums[1])
+            rec["kinetic"].append(sums[2])
+            rec["internal"].append(sums[3])
+            rec["divb"].append(sums[4])
+            if ss.return_radial_momentum:
+                rec["radial"].append(_radial_momentum(dev, config, registered_variables))
         if config.activate_snapshot_callback and snapshot_callable is not None:
-            snapshot_callable(info.t, restore(dev.clone()), registered_variables)
-        k += 1
-        info = plan.run(ptr, prm, 1, stream)
-        _raise_status(info.status, config)
-        steps_taken = info.steps
-        if steps_taken >= max_steps or (not config.fixed_timestep and not (info.t < params.t_end)):
-            break
+            snapshot_callable(t, restore(dev.clone()), registered_variables)
+
+    steps_taken = 0
+    if config.use_specific_snapshot_timepoints and config.return_snapshots:
+        # time_integration.py:542-553, :671-678, :742-750: dt is clipped to the
+        # next requested time point, a snapshot is taken when t is within
+        # 1e-12 of it (at the start of a step), and once more after the step
+        # that reaches t_end; the time points are expected to end at t_end
+        points = [float(v) for v in np.ravel(np.asarray(params.snapshot_timepoints, dtype=np.float64))]
+        k = 0
+        t = 0.0
+        while True:
+            if k < len(points) and abs(t - points[k]) < 1e-12:
+                take(t)
+                k += 1
+            if not (t < params.t_end) or steps_taken >= max_steps:
+                break
+            target = points[min(k, len(points) - 1)] if points else params.t_end
+            if not (target > t):
+                target = params.t_end
+            info = plan.run(ptr, _native.make_params(params._replace(t_end=target)), max_steps - steps_taken, stream)
+            _raise_status(info.status, config)
+            steps_taken = info.steps
+            t = info.t
+            if abs(t - params.t_end) < 1e-12:
+                take(t)
+                break
+    else:
+        # pause before the first step starting at t >= k t_end / n
+        # (time_integration.py:554-566)
+        k = 0
+        while True:
+            thr = k * params.t_end / n if k < n else math.inf
+            info = plan.run_until(ptr, prm, max_steps - steps_taken, thr, stream)
+            _raise_status(info.status, config)
+            steps_taken = info.steps
+            done = (steps_taken >= max_steps) or (not config.fixed_timestep and not (info.t < params.t_end))
+            if done:
+                break
+            take(info.t)
+            k += 1
+            info = plan.run(ptr, prm, 1, stream)
+            _raise_status(info.status, config)
+            steps_taken = info.steps
+            if steps_taken >= max_steps or (not config.fixed_timestep and not (info.t < params.t_end)):
+                break
 
     final = restore(dev)
     if not config.return_snapshots:
@@ -232,20 +268,37 @@ def time_integration(primitive_state, config: SimulationConfig, params: Simulati
     st = None
     if ss.return_states:
         st = np.zeros((n, *shape), dtype=np_dtype)
-        for i, s in enumerate(states[:n]):
-            st[i] = np.asarray(s.cpu() if hasattr(s, "cpu") else s)
+        for i, s_ in enumerate(rec["states"][:n]):
+            st[i] = np.asarray(s_.cpu() if hasattr(s_, "cpu") else s_)
     return SnapshotData(
-        time_points=pad(times),
+        time_points=pad(rec["times"]),
         states=st,
         final_state=final if ss.return_final_state else None,
-        total_mass=pad(mass) if ss.return_total_mass else None,
-        total_energy=pad(energy) if ss.return_total_energy else None,
-        internal_energy=pad(internal) if ss.return_internal_energy else None,
-        kinetic_energy=pad(kinetic) if ss.return_kinetic_energy else None,
-        magnetic_divergence=pad(divb) if (ss.return_magnetic_divergence and config.mhd) else None,
+        total_mass=pad(rec["mass"]) if ss.return_total_mass else None,
+        total_energy=pad(rec["energy"]) if ss.return_total_energy else None,
+        internal_energy=pad(rec["internal"]) if ss.return_internal_energy else None,
+        kinetic_energy=pad(rec["kinetic"]) if ss.return_kinetic_energy else None,
+        radial_momentum=pad(rec["radial"]) if ss.return_radial_momentum else None,
+        magnetic_divergence=pad(rec["divb"]) if (ss.return_magnetic_divergence and config.mhd) else None,
         num_iterations=int(steps_taken),
-        current_checkpoint=min(k, n),
+        current_checkpoint=min(len(rec["times"]), n),
     )
+
+
+def _radial_momentum(dev, config, rv):
+    """calculate_radial_momentum (total_quantities.py:48-71, Cartesian):
+    sum of rho u.r_hat dx^d about the box centre, FP64, on the device."""
+    import torch
+
+    d = int(config.dimensionality)
+    n = dev.shape[-1]
+    dx = float(config.grid_spacing)
+    x = (torch.arange(n, device=dev.device, dtype=torch.float64) + 0.5) * dx - config.box_size / 2
+    grids = torch.meshgrid(*([x] * d), indexing="ij")
+    r = torch.sqrt(sum(g * g for g in grids))
+    rho = dev[rv.density_index].double()
+    ur = sum(dev[1 + i].double() * grids[i] for i in range(d)) / r
+    return float((rho * ur).sum() * (dx ** d if d > 1 else dx))
 
 
 def _raise_status(status, config):

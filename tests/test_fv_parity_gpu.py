@@ -100,3 +100,53 @@ def test_orszag_tang_fp32_l1(cuda):
     ref64 = odriver.time_integration(s.astype(np.float64), cfg, prm, rv)
     assert got.dtype == np.float32
     assert rel_l1(got, ref64) < 1e-5
+
+
+def test_specific_snapshot_timepoints_fp64(cuda):
+    """use_specific_snapshot_timepoints (time_integration.py:542-553, :671-678,
+    :742-750): snapshots exactly at the requested times, each equal to the
+    oracle integrated segment by segment; radial momentum about the box
+    centre (total_quantities.py:48-71)."""
+    from astronomix_gb300 import SnapshotSettings
+    cfg, prm, rv, s = smooth_random(2, 16, seed=21, t_end=0.02)
+    points = (0.0, 0.004, 0.01, 0.02)
+    cfg = cfg._replace(return_snapshots=True, num_snapshots=4, use_specific_snapshot_timepoints=True,
+                       snapshot_settings=SnapshotSettings(return_states=True, return_total_mass=True,
+                                                          return_radial_momentum=True))
+    prm = prm._replace(snapshot_timepoints=points)
+    out = amx.time_integration(s.copy(), cfg, prm, rv)
+    assert np.allclose(out.time_points, points, rtol=0, atol=1e-15)
+    ref = s.copy()
+    base = cfg._replace(return_snapshots=False, use_specific_snapshot_timepoints=False)
+    for i, tp in enumerate(points):
+        if i > 0:
+            ref = odriver.time_integration(ref, base, prm._replace(t_end=tp - points[i - 1]), rv)
+        assert rel_err(out.states[i], ref) < 1e-12, i
+        n = s.shape[-1]
+        x = (np.arange(n) + 0.5) / n - 0.5
+        X, Y = np.meshgrid(x, x, indexing="ij")
+        r = np.sqrt(X ** 2 + Y ** 2)
+        st = out.states[i]
+        radial = (st[0] * (st[1] * X + st[2] * Y) / r).sum() / n ** 2
+        assert out.radial_momentum[i] == pytest.approx(radial, rel=1e-10, abs=1e-14)
+
+
+def test_regular_snapshots_fp64(cuda):
+    """num_snapshots (time_integration.py:554-566): a snapshot at the start of
+    the first step with t >= k t_end / n; the recorded times are the oracle's
+    step times, mass is conserved, and the final state matches."""
+    from astronomix_gb300 import SnapshotSettings
+    cfg, prm, rv, s = orszag_tang(n=32, t_end=0.02)
+    cfg = cfg._replace(return_snapshots=True, num_snapshots=5,
+                       snapshot_settings=SnapshotSettings(return_states=True, return_total_mass=True,
+                                                          return_total_energy=True, return_final_state=True,
+                                                          return_magnetic_divergence=True))
+    out = amx.time_integration(s.copy(), cfg, prm, rv)
+    rec = {}
+    ref = odriver.time_integration(s.copy(), cfg._replace(return_snapshots=False), prm, rv, record=rec)
+    times = np.concatenate([[0.0], np.cumsum(rec["dts"])])
+    expect = [times[np.argmax(times >= k * prm.t_end / 5 - 1e-15)] for k in range(5)]
+    assert np.allclose(out.time_points, expect, rtol=1e-13, atol=1e-15)
+    assert np.allclose(out.total_mass, out.total_mass[0], rtol=1e-13)
+    assert rel_err(out.final_state, ref) < 1e-12
+    assert np.all(out.magnetic_divergence >= 0)
