@@ -61,7 +61,9 @@ int validate(const amx_config* c) {
     if (c->mhd && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
     if (c->split != 0 && c->split != 1) return AMX_ERR_INVALID_ARG;
     if (c->riemann_solver < AMX_HLL || c->riemann_solver > AMX_LAX_FRIEDRICHS) return AMX_ERR_UNSUPPORTED;
-    if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA) return AMX_ERR_UNSUPPORTED;
+    if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA_PP) return AMX_ERR_UNSUPPORTED;
+    // the reference's 1D VAN_ALBADA_PP sums its velocity terms over the whole grid
+    if (c->limiter == AMX_VAN_ALBADA_PP && !c->split && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
     if (c->boundary_handling == AMX_GHOST_CELLS) {
       for (int k = 0; k < c->dimensionality; ++k) {
         for (int side = 0; side < 2; ++side) {
@@ -124,6 +126,7 @@ amx::FVArgs<T> make_fv_args(amx_plan* p, void* state, const amx_params* prm, int
   a.dt_scale = 1.0;
   a.tol = (c.numerical_precision == 1) ? 1e-10 : 1e-5;
   a.max_iters = 1000;
+  a.mhd = c.mhd;
   a.split = c.split;
   a.first_order = c.first_order_fallback;
   a.use_dt_max = c.use_max_adaptive_timestep;
@@ -202,9 +205,13 @@ int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out) 
 
   // ---- FV kernel selection
   const int rs = (cfg->riemann_solver == AMX_HLLC_LM) ? AMX_HLLC : cfg->riemann_solver;
-  const bool ok = (cfg->dtype == AMX_F32) ? amx::fv_kernel_f32(cfg->dimensionality, rs, cfg->mhd != 0, &p->fv)
-                                          : amx::fv_kernel_f64(cfg->dimensionality, rs, cfg->mhd != 0, &p->fv);
+  const int scheme = cfg->split ? amx::FV_SPLIT
+                                 : (cfg->limiter == AMX_VAN_ALBADA_PP ? amx::FV_UNSPLIT_PP : amx::FV_UNSPLIT);
+  const bool ok = (cfg->dtype == AMX_F32)
+                      ? amx::fv_kernel_f32(cfg->dimensionality, rs, cfg->mhd != 0, scheme, &p->fv)
+                      : amx::fv_kernel_f64(cfg->dimensionality, rs, cfg->mhd != 0, scheme, &p->fv);
   if (!ok) { amx_plan_destroy(p); return AMX_ERR_UNSUPPORTED; }
+  if (cfg->limiter == AMX_VAN_ALBADA_PP && !cfg->split) p->fv.smem += p->fv.smem_pp;
   if (cudaFuncSetAttribute(p->fv.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p->fv.smem) != cudaSuccess) {
     amx_plan_destroy(p);
     return AMX_ERR_CUDA;

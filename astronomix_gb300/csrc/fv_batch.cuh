@@ -129,8 +129,11 @@ __device__ __forceinline__ void batch_fold(const T* m, unsigned long long* slot,
   fold_maxima<DIM>(m, slot, red);
 }
 
+// launch bounds as the single-run kernel's, so that the shared per-item
+// functions are compiled under the same register budget (and give the same
+// arithmetic)
 template <typename T, int DIM, int RS, bool MHD, int V>
-__global__ void __launch_bounds__(kFVThreads)
+__global__ void __launch_bounds__(kFVThreads, (DIM == 3 && sizeof(T) == 4) ? 3 : 2)
 fv_batch_kernel(BatchArgs<T> b) {
   using G = TileGeom<T, DIM, V>;
   extern __shared__ __align__(16) unsigned char smem_raw[];

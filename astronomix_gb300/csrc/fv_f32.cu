@@ -6,12 +6,14 @@ namespace amx {
 
 #define AMX_FV_CASE(D, R, M)                                                  \
   if (dim == D && rs == R && mhd == M) {                                      \
-    out->fn = (const void*)&fv_run_kernel<float, D, R, M>;                    \
+    out->fn = (const void*)&fv_run_kernel<float, D, R, M, FV_UNSPLIT>;                    \
     out->smem = TileGeom<float, D>::SMEM;                                     \
+    out->smem_pp = TileGeom<float, D>::PP_SMEM;                               \
     return true;                                                              \
   }
 
-bool fv_kernel_f32(int dim, int rs, bool mhd, FVKernelInfo* out) {
+bool fv_kernel_f32(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out) {
+  if (scheme != FV_UNSPLIT) return fv_kernel_f32_schemes(dim, rs, mhd, scheme, out);
   AMX_FV_CASE(1, RS_HLL, false)
   AMX_FV_CASE(1, RS_HLLC, false)
   AMX_FV_CASE(1, RS_LF, false)

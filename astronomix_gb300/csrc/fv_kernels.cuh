@@ -43,6 +43,8 @@ struct FVControl {
   int status;
 };
 
+enum FVScheme { FV_UNSPLIT = 0, FV_SPLIT = 1, FV_UNSPLIT_PP = 2 };
+
 enum FVMode {
   FV_MODE_STEPS = 0,      // full time steps
   FV_MODE_CFL = 1,        // only the CFL dt (written to ctl->dt)
@@ -81,6 +83,7 @@ struct FVArgs {
   double dt_scale;   // seam modes
   double tol;        // fixed-point tolerance
   int max_iters;     // fixed-point cap (1000 in the reference)
+  int mhd;           // the state carries B (the magnetic split is active)
   int split;         // 1: dimensionally split MUSCL-Hancock sweeps instead of SSP-RK2
   int first_order;   // split: piecewise-constant interface states
   int use_dt_max;    // split: dt = min(dt, dt_max)
@@ -161,6 +164,11 @@ struct TileGeom {
   static constexpr size_t HYDRO_SMEM = sizeof(T) * (size_t)NV * (HALO + FREG + SREG);
   static constexpr size_t MAG_SMEM = sizeof(T) * (size_t)6 * MHALO;
   static constexpr size_t SMEM = HYDRO_SMEM > MAG_SMEM ? HYDRO_SMEM : MAG_SMEM;
+  // VAN_ALBADA_PP: the limited differences of every axis for the tile and a
+  // halo of 1, after the hydro arrays
+  static constexpr int B0 = T0 + 2, B1 = (DIM >= 2) ? T1 + 2 : 1, B2 = (DIM >= 3) ? T2 + 2 : 1;
+  static constexpr int BOX = B0 * B1 * B2;
+  static constexpr size_t PP_SMEM = sizeof(T) * (size_t)DIM * NV * BOX;
 };
 
 template <int DIM>
@@ -253,6 +261,89 @@ __device__ __noinline__ void phase_cfl(const FVArgs<T>& a, const T* st, unsigned
 
 // ------------------------------------------------------------ hydro stage
 
+// The VAN_ALBADA_PP rescaling of one cell's differences d[k][v] (limited
+// gradient x dx/2 along axis k) for positivity (reconstruction.py:167-362):
+// the density and pressure differences of axis k by alpha_k, kappa_k, the
+// velocity differences by one beta per cell.  C[k] = a_k / sum(a) from the
+// global maxima a_k of |u_k| + c; q = 2 / C_cfl with MHD, 1 / C_cfl
+// without.  A1 pairs C, alpha and the density difference of axis j with
+// velocity component j, as the reference's array broadcasting does.
+template <typename T, int DIM>
+__device__ __forceinline__ void pp_limit(T (*d)[DIM + 2], T rho, T p, const T* C, T q, T gamma) {
+  constexpr int P = DIM + 1;
+  const T eps = T(1e-14);
+  T alpha[DIM], kappa[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    const T dr = d[k][0], dp = d[k][P];
+    alpha[k] = Num<T>::abs_(dr) > eps ? jmin(rho / (Num<T>::abs_(dr) * (T(1) + eps)), T(1)) : T(1);
+    kappa[k] = Num<T>::abs_(dp) > eps ? jmin(p / (Num<T>::abs_(dp) * (T(1) + eps)), T(1)) : T(1);
+  }
+  T A1 = T(0), A2 = T(0), vsum = T(0);
+#pragma unroll
+  for (int j = 0; j < DIM; ++j) {
+    const T X = C[j] * alpha[j] * d[j][0];
+    T S = X * d[0][1 + j];
+#pragma unroll
+    for (int k = 1; k < DIM; ++k) S = S + X * d[k][1 + j];
+    A1 = (j == 0) ? S * S : A1 + S * S;
+  }
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    T sq = d[k][1] * d[k][1];
+#pragma unroll
+    for (int j = 1; j < DIM; ++j) sq = sq + d[k][1 + j] * d[k][1 + j];
+    A2 = (k == 0) ? C[k] * sq : A2 + C[k] * sq;
+    vsum = (k == 0) ? sq : vsum + sq;
+  }
+  const bool moving = vsum > eps;
+  if (!moving) { A1 = eps; A2 = eps; }
+  const T qm2 = q - T(2);
+  const T beta = moving ? jmin(Num<T>::sqrt_((qm2 * qm2 * rho * p) /
+                                             ((gamma - T(1)) * (T(2) * A1 + qm2 * (rho * rho) * A2))), T(1))
+                        : T(1);
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    d[k][0] = d[k][0] * alpha[k];
+    d[k][P] = d[k][P] * kappa[k];
+#pragma unroll
+    for (int j = 0; j < DIM; ++j) d[k][1 + j] = d[k][1 + j] * beta;
+  }
+}
+
+// VAN_ALBADA_PP pre-pass of a hydro tile: the rescaled differences of every
+// axis for the tile and a halo of 1 from the staged primitives sP into sPP
+// ([DIM][NV][BOX]).  Out of line, so that the registers it needs do not
+// weigh on the hydro stage of the other limiters.
+template <typename T, int DIM, int V>
+__device__ __noinline__ void pp_prepass(const FVArgs<T>& a, const T* sP, T* sPP, const T* ppC) {
+  using G = TileGeom<T, DIM, V>;
+  constexpr int NV = G::NV;
+  const T gamma = T(a.gamma);
+  const T dxT = T(a.dx);
+  const int limiter = a.limiter;
+  const T q = T(a.mhd ? 2 : 1) / T(a.C_cfl);  // the hydro half steps of the MHD split count as C_cfl / 2
+  for (int e = threadIdx.x; e < G::BOX; e += blockDim.x) {
+    const int b2 = e % G::B2, b1 = (e / G::B2) % G::B1, b0 = e / (G::B2 * G::B1);
+    const int hh = ((b0 + 1) * G::H1 + (DIM >= 2 ? b1 + 1 : 0)) * G::H2 + (DIM >= 3 ? b2 + 1 : 0);
+    T d[DIM][DIM + 2];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const T* s = sP + v * G::HALO + hh;
+        d[k][v] = limited((s[0] - s[-stride]) / dxT, (s[stride] - s[0]) / dxT, limiter, dxT) * dxT / T(2);
+      }
+    }
+    pp_limit<T, DIM>(d, sP[hh], sP[(NV - 1) * G::HALO + hh], ppC, q, gamma);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) sPP[(k * NV + v) * G::BOX + e] = d[k][v];
+  }
+}
+
 // One _evolve_gas_state_unsplit_inner (evolve_state.py:339-414):
 //   U = cons(P_in); for each axis: U += (1/dx) (F[i-1/2] - F[i+1/2]) dt;
 //   P_out = prim(U)
@@ -262,9 +353,10 @@ __device__ __noinline__ void phase_cfl(const FVArgs<T>& a, const T* st, unsigned
 // limited slope of every cell (reconstruction.py:399-431) is computed once
 // per axis into shared memory and read by both of its faces.  The maxima of
 // |u_a| + c of P_out are folded into `out_slot`.
-template <typename T, int DIM, int RS, int V = 0>
+template <typename T, int DIM, int RS, int V = 0, bool PP = false>
 __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, const T* __restrict__ Pin, T* Pout,
-                                           const T* P0, T dt, const T* alpha, T* smem, T* m, bool track) {
+                                           const T* P0, T dt, const T* alpha, T* smem, T* m, bool track,
+                                           const T* ppC = nullptr) {
   using G = TileGeom<T, DIM, V>;
   constexpr int NV = G::NV;
   const int n = a.n;
@@ -298,6 +390,14 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
   }
   __syncthreads();
 
+  // ---- VAN_ALBADA_PP: the rescaled differences of every axis for the tile
+  // and a halo of 1, before any face needs them (reconstruction.py:134-394)
+  T* sPP = smem + NV * (G::HALO + G::FREG + G::SREG);  // [DIM][NV][BOX]
+  if (PP) {
+    pp_prepass<T, DIM, V>(a, sP, sPP, ppC);
+    __syncthreads();
+  }
+
   // ---- per-thread cells: conserved state from the (mapped) primitives
   T U[G::CPT][NV];
 #pragma unroll
@@ -320,7 +420,7 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
 #pragma unroll
   for (int pass = 0; pass < NPASS; ++pass) {
     const int k_lo = G::FUSED ? 0 : pass, k_hi = G::FUSED ? DIM : pass + 1;
-    for (int k = k_lo; k < (G::SLOPES ? k_hi : k_lo); ++k) {
+    for (int k = k_lo; k < ((G::SLOPES && !PP) ? k_hi : k_lo); ++k) {
       const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
       const int D0 = G::T0 + 2 * (k == 0), D1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1,
                 D2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
@@ -339,7 +439,7 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
         }
       }
     }
-    if (G::SLOPES) __syncthreads();
+    if (G::SLOPES && !PP) __syncthreads();
     for (int k = k_lo; k < k_hi; ++k) {
       const int stride = (k == 0) ? G::H1 * G::H2 : ((k == 1) ? G::H2 : 1);
       const int D1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1, D2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
@@ -362,7 +462,14 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
           const T* s = sP + v * G::HALO + h;
-          if (G::SLOPES) {
+          if (PP) {
+            // box index of the cell right of the face, and of its left neighbour along k
+            const int br = ((f0 + 1) * G::B1 + (DIM >= 2 ? f1 + 1 : 0)) * G::B2 + (DIM >= 3 ? f2 + 1 : 0);
+            const int bl = br - ((k == 0) ? G::B1 * G::B2 : ((k == 1) ? G::B2 : 1));
+            const T* dd = sPP + (k * NV + v) * G::BOX;
+            qL[v] = s[-stride] + dd[bl];
+            qR[v] = s[0] - dd[br];
+          } else if (G::SLOPES) {
             const T* d = sDk + v * sdim + ds;
             qL[v] = s[-stride] + d[-dstride];
             qR[v] = s[0] - d[0];
@@ -431,17 +538,17 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
   if (G::FUSED) __syncthreads();  // the flux arrays are read above; the next tile overwrites them
 }
 
-template <typename T, int DIM, int RS>
+template <typename T, int DIM, int RS, bool PP = false>
 __device__ __noinline__ void phase_hydro_stage(const FVArgs<T>& a, const T* __restrict__ Pin, T* Pout,
                                                const T* P0, T dt, const T* alpha, T* smem,
-                                               unsigned long long* out_slot, double* red) {
+                                               unsigned long long* out_slot, double* red, const T* ppC = nullptr) {
   using G = TileGeom<T, DIM>;
   const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
   T m[3] = {T(0), T(0), T(0)};
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int o[3];
     tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
-    FVItems<T, DIM, RS, 0>::hydro(a, o, Pin, Pout, P0, dt, alpha, smem, m, out_slot != nullptr);
+    FVItems<T, DIM, RS, 0>::template hydro<PP>(a, o, Pin, Pout, P0, dt, alpha, smem, m, out_slot != nullptr, ppC);
   }
   if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
@@ -907,17 +1014,20 @@ __device__ __forceinline__ void mag_finalize_cell(const T* state, T* out, long l
 // division, straight-line code) inlining already gives identical results.
 template <typename T, int DIM, int RS, int V>
 struct FVItems {
+  template <bool PP = false>
   static __device__ __forceinline__ void hydro(const FVArgs<T>& a, const int* o, const T* Pin, T* Pout,
-                                               const T* P0, T dt, const T* alpha, T* smem, T* m, bool track) {
-    hydro_tile<T, DIM, RS, V>(a, o, Pin, Pout, P0, dt, alpha, smem, m, track);
+                                               const T* P0, T dt, const T* alpha, T* smem, T* m, bool track,
+                                               const T* ppC = nullptr) {
+    hydro_tile<T, DIM, RS, V, PP>(a, o, Pin, Pout, P0, dt, alpha, smem, m, track, ppC);
   }
 };
 template <int DIM, int RS, int V>
 struct FVItems<double, DIM, RS, V> {
+  template <bool PP = false>
   static __device__ __noinline__ void hydro(const FVArgs<double>& a, const int* o, const double* Pin, double* Pout,
                                             const double* P0, double dt, const double* alpha, double* smem,
-                                            double* m, bool track) {
-    hydro_tile<double, DIM, RS, V>(a, o, Pin, Pout, P0, dt, alpha, smem, m, track);
+                                            double* m, bool track, const double* ppC = nullptr) {
+    hydro_tile<double, DIM, RS, V, PP>(a, o, Pin, Pout, P0, dt, alpha, smem, m, track, ppC);
   }
 };
 
@@ -973,7 +1083,10 @@ __device__ __noinline__ void phase_mag_finalize(const FVArgs<T>& a, const T* sta
 
 // 3D is bound by HBM latency: its FP32 instantiations are held to three resident
 // blocks per SM (85 registers), 1D and 2D to two (128 registers).
-template <typename T, int DIM, int RS, bool MHD>
+// SCHEME: FV_UNSPLIT, FV_SPLIT (MUSCL-Hancock sweeps) or FV_UNSPLIT_PP
+// (VAN_ALBADA_PP reconstruction); a compile-time choice, so that the
+// ordinary scheme's kernel carries none of the others' code.
+template <typename T, int DIM, int RS, bool MHD, int SCHEME = FV_UNSPLIT>
 __global__ void __launch_bounds__(kFVThreads, (DIM == 3 && sizeof(T) == 4) ? 3 : 2)
 fv_run_kernel(FVArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -986,6 +1099,10 @@ fv_run_kernel(FVArgs<T> a) {
   T* gas = a.state;
   constexpr int NVG_ = DIM + 2;
   __shared__ T s_alpha[3];
+  __shared__ T s_ppC[3];
+  // VAN_ALBADA_PP (unsplit): every stage needs C_k from the maxima of its input
+  constexpr bool pp = (SCHEME == FV_UNSPLIT_PP) && DIM >= 2;
+  constexpr bool split = (SCHEME == FV_SPLIT);
 
   // Producer ring of maxima: the phase with pass number rp writes slot rp % 3
   // after block 0 cleared slot (rp + 1) % 3; the slot a phase reads is the
@@ -1002,10 +1119,18 @@ fv_run_kernel(FVArgs<T> a) {
     for (int k = 0; k < 3; ++k) m[k] = (k < DIM) ? bits_to_double(s[k]) : 0.0;
   };
   auto set_alpha = [&]() {
-    if (RS != RS_LF) return;
+    if (RS != RS_LF && !pp) return;
     double m[3];
     last_maxima(m);
-    if (threadIdx.x < DIM) s_alpha[threadIdx.x] = T(m[threadIdx.x]);
+    if (RS == RS_LF && threadIdx.x < DIM) s_alpha[threadIdx.x] = T(m[threadIdx.x]);
+    if (pp && threadIdx.x == 0) {  // (pp is a compile-time constant)
+      // C = alpha_lax / sum(alpha_lax) (reconstruction.py:172-182)
+      T tot = T(m[0]);
+#pragma unroll
+      for (int k = 1; k < DIM; ++k) tot = tot + T(m[k]);
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) s_ppC[k] = T(m[k]) / tot;
+    }
     __syncthreads();
   };
   // `need`: whether anything reads the maxima of this stage's output (the
@@ -1013,8 +1138,12 @@ fv_run_kernel(FVArgs<T> a) {
   auto stage = [&](const T* in, T* out, const T* p0, T h, bool need) -> bool {
     set_alpha();
     unsigned long long* slot = produce_slot();
-    phase_hydro_stage<T, DIM, RS>(a, in, out, p0, h, RS == RS_LF ? s_alpha : nullptr, smem,
-                                  (need || RS == RS_LF) ? slot : nullptr, red);
+    if constexpr (pp)
+      phase_hydro_stage<T, DIM, RS, true>(a, in, out, p0, h, RS == RS_LF ? s_alpha : nullptr, smem, slot, red,
+                                          s_ppC);
+    else
+      phase_hydro_stage<T, DIM, RS>(a, in, out, p0, h, RS == RS_LF ? s_alpha : nullptr, smem,
+                                    (need || RS == RS_LF) ? slot : nullptr, red);
     ++rp;
     return grid_sync(bar, status);
   };
@@ -1028,8 +1157,9 @@ fv_run_kernel(FVArgs<T> a) {
   auto sweep = [&](const T* in, T* out, int k, T h, bool need) -> bool {
     set_alpha();
     unsigned long long* slot = produce_slot();
-    phase_sweep<T, DIM, RS>(a, k, in, out, h, RS == RS_LF ? s_alpha : nullptr, smem,
-                            (need || RS == RS_LF) ? slot : nullptr, red);
+    if constexpr (split)
+      phase_sweep<T, DIM, RS>(a, k, in, out, h, RS == RS_LF ? s_alpha : nullptr, smem,
+                              (need || RS == RS_LF) ? slot : nullptr, red);
     ++rp;
     return grid_sync(bar, status);
   };
@@ -1038,6 +1168,9 @@ fv_run_kernel(FVArgs<T> a) {
   // rotating through the state, p1 and p2 so that the last one lands in the
   // state; in 1D the single sweep's result is copied back
   auto split_update = [&](T h, bool last) -> bool {
+    if constexpr (!split) {
+      return false;
+    } else {
     if (DIM == 1) {
       if (!sweep(gas, a.p1, 0, h, last)) return false;
       const long long total = (long long)NVG_ * nc;
@@ -1057,9 +1190,13 @@ fv_run_kernel(FVArgs<T> a) {
     if (!sweep(a.p2, a.p1, 2, h, false)) return false;
     if (!sweep(a.p1, a.p2, 1, h2, false)) return false;
     return sweep(a.p2, gas, 0, h2, last);
+    }
   };
   // the gas update of the configured scheme
-  auto rk2 = [&](T h, bool last) -> bool { return a.split ? split_update(h, last) : rk2_unsplit(h, last); };
+  auto rk2 = [&](T h, bool last) -> bool {
+    if constexpr (split) return split_update(h, last);
+    else return rk2_unsplit(h, last);
+  };
 
   // magnetic_update (_magnetic_field_update.py:37-242); returns iterations or -1
   auto magnetic = [&](T h) -> int {
@@ -1095,7 +1232,7 @@ fv_run_kernel(FVArgs<T> a) {
     if (change > a.tol && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_NOT_CONVERGED);
     if (change != change && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_NAN);
     unsigned long long* out = produce_slot();
-    phase_mag_finalize<T, DIM>(a, gas, cur, gas, RS == RS_LF ? out : nullptr, red);
+    phase_mag_finalize<T, DIM>(a, gas, cur, gas, (RS == RS_LF || pp) ? out : nullptr, red);
     ++rp;
     if (!grid_sync(bar, status)) return -1;
     return it;
@@ -1107,7 +1244,7 @@ fv_run_kernel(FVArgs<T> a) {
   auto dt_from_maxima = [&]() -> double {
     double m[3];
     last_maxima(m);
-    if (a.split) {
+    if constexpr (split) {
       double w = m[0];
 #pragma unroll
       for (int k = 1; k < DIM; ++k) w = nanmax(w, m[k]);

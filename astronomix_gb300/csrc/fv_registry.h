@@ -7,10 +7,15 @@ namespace amx {
 struct FVKernelInfo {
   const void* fn;      // __global__ function
   size_t smem;         // dynamic shared memory per block
+  size_t smem_pp;      // extra shared memory with the VAN_ALBADA_PP limiter
 };
 
 // riemann family: 0 = HLL, 1 = HLLC (and HLLC-LM), 3 = Lax-Friedrichs
-bool fv_kernel_f32(int dim, int rs, bool mhd, FVKernelInfo* out);
-bool fv_kernel_f64(int dim, int rs, bool mhd, FVKernelInfo* out);
+// scheme: FV_UNSPLIT, FV_SPLIT or FV_UNSPLIT_PP (fv_kernels.cuh)
+bool fv_kernel_f32(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out);
+bool fv_kernel_f64(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out);
+// the split and VAN_ALBADA_PP instantiations (own translation units)
+bool fv_kernel_f32_schemes(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out);
+bool fv_kernel_f64_schemes(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out);
 
 }  // namespace amx

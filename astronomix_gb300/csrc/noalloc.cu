@@ -118,6 +118,7 @@ int launch(const amx_config* c, void* state, const amx_params* prm, int64_t max_
   a.dt_in = 0.0;
   a.dt_scale = 1.0;
   a.tol = (c->numerical_precision == 1) ? 1e-10 : 1e-5;
+  a.mhd = c->mhd;
   a.split = c->split;
   a.first_order = c->first_order_fallback;
   a.use_dt_max = c->use_max_adaptive_timestep;
@@ -163,8 +164,9 @@ extern "C" int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_
 
   amx::FVKernelInfo kinfo{};
   const int rs = (cfg->riemann_solver == AMX_HLLC_LM) ? AMX_HLLC : cfg->riemann_solver;
-  const bool ok = (cfg->dtype == AMX_F32) ? amx::fv_kernel_f32(cfg->dimensionality, rs, cfg->mhd != 0, &kinfo)
-                                          : amx::fv_kernel_f64(cfg->dimensionality, rs, cfg->mhd != 0, &kinfo);
+  const int scheme = cfg->split ? amx::FV_SPLIT : amx::FV_UNSPLIT;
+  const bool ok = (cfg->dtype == AMX_F32) ? amx::fv_kernel_f32(cfg->dimensionality, rs, cfg->mhd != 0, scheme, &kinfo)
+                                          : amx::fv_kernel_f64(cfg->dimensionality, rs, cfg->mhd != 0, scheme, &kinfo);
   if (!ok) return AMX_ERR_UNSUPPORTED;
   if (cudaFuncSetAttribute(kinfo.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kinfo.smem) != cudaSuccess)
     return AMX_ERR_CUDA;

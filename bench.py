@@ -50,14 +50,15 @@ def parse():
     ap.add_argument("--no-arena", action="store_true", help="skip the 256^3 blast comparison")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-run batched ensemble")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 128^3 adjoint workload")
-    ap.add_argument("--case", default=None, choices=["fd", "ensemble", "adjoint"],
+    ap.add_argument("--case", default=None, choices=["fd", "fv3d", "ensemble", "adjoint"],
                     help="run one small case of a secondary workload and exit (for profilers)")
     return ap.parse_args()
 
 
 def run_case(name):
     """Small, self-contained runs of the secondary workloads for ncu captures:
-    fd: FD WENO-CT blast 128^3 FP32, 2 steps; ensemble: 8 turbulent 2D MHD
+    fd: FD WENO-CT blast 128^3 FP32, 2 steps; fv3d: FV Lax-Friedrichs MHD
+    blast 192^3 FP32, 2 steps (one launch); ensemble: 8 turbulent 2D MHD
     runs (128^2..512^2, t_end / 8) in one batched launch; adjoint: the 3D
     density-perturbation problem at 96^3 to t = 0.01, forward and backward
     with the stored tape (a 4 GB tape budget: the case holds a few GB at
@@ -65,10 +66,10 @@ def run_case(name):
     import torch
     from astronomix_gb300 import _native
 
-    if name == "fd":
+    if name in ("fd", "fv3d"):
         from astronomix_gb300.time_integration import get_plan
 
-        cfg, prm, rv, s = arena_blast(128, "fd")
+        cfg, prm, rv, s = arena_blast(128 if name == "fd" else 192, name[:2])
         plan = get_plan(cfg, rv, s.shape, np.float32)
         dev = torch.from_numpy(s).cuda()
         st = torch.cuda.current_stream().cuda_stream

@@ -55,6 +55,7 @@ extern "C" {
 #define AMX_DOUBLE_MINMOD 2
 #define AMX_SUPERBEE 3
 #define AMX_VAN_ALBADA 4
+#define AMX_VAN_ALBADA_PP 5  /* positivity-preserving multidimensional (unsplit, 2D / 3D) */
 
 #define AMX_BC_OPEN 0
 #define AMX_BC_REFLECTIVE 1
@@ -76,7 +77,7 @@ typedef struct amx_config {
   int32_t num_vars;               /* rows of the state array                    */
   int32_t mhd;                    /* 0 / 1                                      */
   int32_t riemann_solver;         /* AMX_HLL .. AMX_LAX_FRIEDRICHS              */
-  int32_t limiter;                /* AMX_MINMOD .. AMX_VAN_ALBADA               */
+  int32_t limiter;                /* AMX_MINMOD .. AMX_VAN_ALBADA_PP            */
   int32_t fv_magnetic_integrator; /* AMX_IMPLICIT_MIDPOINT / _EULER             */
   int32_t numerical_precision;    /* 0: fixed-point tol 1e-5, 1: 1e-10          */
   int32_t boundary_handling;      /* AMX_GHOST_CELLS / AMX_PERIODIC_ROLL        */

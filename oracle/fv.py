@@ -13,7 +13,7 @@ reference's ``axis`` argument) is array axis ``a``.
 
 from astronomix_gb300.option_classes import (
     GHOST_CELLS, OPEN_BOUNDARY, REFLECTIVE_BOUNDARY, PERIODIC_BOUNDARY,
-    MINMOD, OSHER, DOUBLE_MINMOD, SUPERBEE, VAN_ALBADA,
+    MINMOD, OSHER, DOUBLE_MINMOD, SUPERBEE, VAN_ALBADA, VAN_ALBADA_PP,
     HLL, HLLC, HLLC_LM, LAX_FRIEDRICHS, UNSPLIT, RK2_SSP, MUSCL,
     IMPLICIT_MIDPOINT, IMPLICIT_EULER, SINGLE_PRECISION, DOUBLE_PRECISION,
 )
@@ -281,7 +281,7 @@ def limited_gradients(P, config, axis):
         return _superbee(bd, fd)
     if lim == DOUBLE_MINMOD:
         return _double_minmod(bd, fd)
-    if lim == VAN_ALBADA:
+    if lim in (VAN_ALBADA, VAN_ALBADA_PP):
         return _van_albada(bd, fd, dx)
     if lim == OSHER:
         eps = 1e-11
@@ -334,6 +334,75 @@ def reconstruct_split(P, dt, gamma, config, rv, axis):
     left = predictors - dist * g
     right = predictors + dist * g
     return xp.roll(right, 1, axis), left
+
+
+def reconstruct_unsplit_pp(P, gamma, config, rv, C_cfl):
+    """reconstruction.py:134-394, the VAN_ALBADA_PP branch (2D / 3D): van
+    Albada differences along every axis, rescaled per cell for positivity.
+    C_k = alpha_k / sum(alpha) from the global maxima of |u_k| + c; the
+    density and pressure differences of axis k are limited by alpha_k,
+    kappa_k; the velocity differences by one beta per cell, whose A1 pairs
+    the axis-j factors with velocity component j (the reference's
+    broadcasting of C * alpha * d_rho against the (axis, component) array of
+    velocity differences).  Returns [(p_left_interface, p_right_interface)]
+    per axis."""
+    dims = config.dimensionality
+    if dims < 2:
+        raise NotImplementedError("VAN_ALBADA_PP in 1D sums over the whole grid in the reference; "
+                                  "not part of the accelerated path")
+    eps = 1e-14
+    d = [limited_gradients(P, config, axis) * config.grid_spacing / 2 for axis in range(1, dims + 1)]
+    ri, pi = rv.density_index, rv.pressure_index
+    rho = P[ri]
+    p = P[pi]
+    c = speed_of_sound(rho, p, gamma)
+    alpha_lax = [xp.amax(xp.abs(P[axis]) + c) for axis in range(1, dims + 1)]
+    tot = alpha_lax[0]
+    for a_ in alpha_lax[1:]:
+        tot = tot + a_
+    C = [a_ / tot for a_ in alpha_lax]
+    q = (2 / C_cfl) if config.mhd else (1 / C_cfl)
+
+    def limit(x, ref):
+        prot = xp.where(xp.abs(x) > eps, x, eps)
+        return xp.where(xp.abs(x) > eps, xp.minimum(ref / (xp.abs(prot) * (1 + eps)), 1), 1)
+
+    alpha_d = [limit(d[k][ri], rho) for k in range(dims)]
+    kappa_p = [limit(d[k][pi], p) for k in range(dims)]
+    A1 = None
+    for j in range(dims):
+        X = C[j] * alpha_d[j] * d[j][ri]
+        S = None
+        for k in range(dims):
+            term = X * d[k][1 + j]
+            S = term if S is None else S + term
+        A1 = S ** 2 if A1 is None else A1 + S ** 2
+    A2 = None
+    vsum = None
+    for k in range(dims):
+        sq_ = None
+        for j in range(dims):
+            t_ = d[k][1 + j] ** 2
+            sq_ = t_ if sq_ is None else sq_ + t_
+        term = C[k] * sq_
+        A2 = term if A2 is None else A2 + term
+        vsum = sq_ if vsum is None else vsum + sq_
+    A1 = xp.where(vsum > eps, A1, eps)
+    A2 = xp.where(vsum > eps, A2, eps)
+    beta = xp.where(vsum > eps,
+                    xp.minimum(xp.sqrt(((q - 2) ** 2 * rho * p) / ((gamma - 1) * (2 * A1 + (q - 2) * rho ** 2 * A2))),
+                               1), 1)
+    out = []
+    for k in range(dims):
+        dk = xp.copy(d[k])
+        dk[ri] = d[k][ri] * alpha_d[k]
+        dk[pi] = d[k][pi] * kappa_p[k]
+        for j in range(dims):
+            dk[1 + j] = d[k][1 + j] * beta
+        left_center = P - dk
+        right_center = P + dk
+        out.append((xp.roll(right_center, 1, k + 1), left_center))
+    return out
 
 
 # ------------------------------------------------------ Riemann solvers
@@ -427,17 +496,21 @@ def riemann_solver(PL, PR, P, gamma, config, rv, d):
 
 # ------------------------------------------------------- hydro stepper
 
-def evolve_gas_unsplit_inner(P, dt, gamma, config, rv):
+def evolve_gas_unsplit_inner(P, dt, gamma, config, rv, C_cfl=None):
     """_finite_volume/_state_evolution/evolve_state.py:339-414."""
     dims = config.dimensionality
     ghost = config.boundary_handling == GHOST_CELLS
     if ghost:
         P = boundary_handler(P, config)
     U = conserved_state_from_primitive(P, gamma, dims, rv)
+    pp = reconstruct_unsplit_pp(P, gamma, config, rv, C_cfl) if config.limiter == VAN_ALBADA_PP else None
     for axis in range(1, dims + 1):
         if ghost:
             P = boundary_handler(P, config)
-        PL, PR = reconstruct_unsplit_single(P, config, axis)
+        if pp is not None:
+            PL, PR = pp[axis - 1]
+        else:
+            PL, PR = reconstruct_unsplit_single(P, config, axis)
         F = riemann_solver(PL, PR, P, gamma, config, rv, axis)
         U = U + 1 / config.grid_spacing * (F - xp.roll(F, -1, axis)) * dt
     P = primitive_state_from_conserved(U, gamma, dims, rv)
@@ -446,13 +519,13 @@ def evolve_gas_unsplit_inner(P, dt, gamma, config, rv):
     return P
 
 
-def evolve_gas_unsplit(P, dt, gamma, config, rv):
+def evolve_gas_unsplit(P, dt, gamma, config, rv, C_cfl=None):
     """evolve_state.py:419-488 (SSP-RK2 / Heun in conserved variables)."""
     if config.time_integrator != RK2_SSP:
         raise ValueError("Only the RK2 SSP time integrator is supported for the unsplit scheme.")
     dims = config.dimensionality
-    P1 = evolve_gas_unsplit_inner(P, dt, gamma, config, rv)
-    P2 = evolve_gas_unsplit_inner(P1, dt, gamma, config, rv)
+    P1 = evolve_gas_unsplit_inner(P, dt, gamma, config, rv, C_cfl)
+    P2 = evolve_gas_unsplit_inner(P1, dt, gamma, config, rv, C_cfl)
     U0 = conserved_state_from_primitive(P, gamma, dims, rv)
     U2 = conserved_state_from_primitive(P2, gamma, dims, rv)
     U = 0.5 * (U0 + U2)
@@ -494,9 +567,9 @@ def evolve_gas_split(P, dt, gamma, config, rv):
     return evolve_along_axis(P, dt / 2, gamma, config, rv, 1)
 
 
-def evolve_gas(P, dt, gamma, config, rv):
+def evolve_gas(P, dt, gamma, config, rv, C_cfl=None):
     if config.split == UNSPLIT:
-        return evolve_gas_unsplit(P, dt, gamma, config, rv)
+        return evolve_gas_unsplit(P, dt, gamma, config, rv, C_cfl)
     return evolve_gas_split(P, dt, gamma, config, rv)
 
 
@@ -631,20 +704,21 @@ def magnetic_update(B, gas, dx, dt, config, rv, return_iterations=False):
     return Bn, gas
 
 
-def evolve_state_fv(P, dt, gamma, config, rv, stats=None):
-    """evolve_state.py:497-600 (unsplit or split gas scheme; MHD via the Pang-Wu split)."""
+def evolve_state_fv(P, dt, gamma, config, rv, stats=None, C_cfl=None):
+    """evolve_state.py:497-600 (unsplit or split gas scheme; MHD via the Pang-Wu split).
+    C_cfl is needed by the VAN_ALBADA_PP reconstruction only."""
     if not config.mhd:
-        return evolve_gas(P, dt, gamma, config, rv)
+        return evolve_gas(P, dt, gamma, config, rv, C_cfl)
     if config.dimensionality < 2:
         raise ValueError("MHD currently not supported in 1D.")
     rv_gas = rv._replace(num_vars=rv.num_vars - 3)
     gas = P[:-3]
     B = P[-3:]
-    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas)
+    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas, C_cfl)
     B, gas, it = magnetic_update(B, gas, config.grid_spacing, dt, config, rv, return_iterations=True)
     if stats is not None:
         stats.append(it)
-    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas)
+    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas, C_cfl)
     return xp.concatenate([gas, B], axis=0)
 
 
