@@ -18,9 +18,10 @@ from .option_classes import (
     CARTESIAN, CYLINDRICAL, SPHERICAL,
     GHOST_CELLS, PERIODIC_ROLL, IMPLICIT_MIDPOINT, IMPLICIT_EULER,
     SINGLE_PRECISION, DOUBLE_PRECISION, WindParams,
+    SIMPLE_SOURCE_TERM, DONOR_ACCOUNTING, RIEMANN_SPLIT, RIEMANN_SPLIT_UNSTABLE, HALF_SPLIT,
 )
 from .variable_registry import get_registered_variables, RegisteredVariables, StaticIntVector
 from .setup_helpers import get_helper_data, construct_primitive_state, initialize_interface_fields, HelperData
-from .time_integration import time_integration, SnapshotData, StateStruct
+from .time_integration import time_integration, gravitational_potential, SnapshotData, StateStruct
 
 __version__ = "0.1.0"

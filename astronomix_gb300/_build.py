@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--ex
 # the slowest units first, so that the parallel build finishes early
 SOURCES = ["fv_f32_schemes.cu", "fv_f64_schemes.cu", "fv_batch_f32.cu", "fv_batch_f32_alt.cu", "adjoint_f32.cu",
            "adjoint_f64.cu", "amx_api.cu", "fv_f32.cu", "fv_f64.cu", "fd.cu", "fd_f32.cu", "fd_f64.cu",
-           "fv_batch_f64.cu", "batch.cu", "adjoint.cu", "diag.cu"]
+           "fv_batch_f64.cu", "batch.cu", "adjoint.cu", "gravity.cu", "diag.cu"]
 
 # FP32 FV kernels use approximate division and square root: the FP32 path is
 # held to an L1 tolerance against FP64, while the FP64 units keep IEEE
@@ -93,7 +93,8 @@ def build(verbose: bool = False, jobs: int = 0) -> str:
             list(ex.map(compile_one, todo))
     if todo or _mtime(LIB) < max(_mtime(o) for o in objs):
         tmp = LIB + ".tmp"
-        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
+        cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "lib64")
+        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-L" + cudalib, "-lcufft", "-Xlinker", "-rpath=" + cudalib]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

@@ -68,6 +68,8 @@ class amx_config(ctypes.Structure):
         ("split", ctypes.c_int32),
         ("first_order_fallback", ctypes.c_int32),
         ("use_max_adaptive_timestep", ctypes.c_int32),
+        ("self_gravity", ctypes.c_int32),
+        ("self_gravity_version", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
     ]
 
@@ -80,6 +82,7 @@ class amx_params(ctypes.Structure):
         ("minimum_pressure", ctypes.c_double),
         ("dt_max", ctypes.c_double),
         ("t_end", ctypes.c_double),
+        ("gravitational_constant", ctypes.c_double),
     ]
 
 
@@ -141,6 +144,9 @@ SIGNATURES = {
     "amx_adjoint_schedule": (_I32, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I32), _I64, ctypes.POINTER(_I64)]),
     "amx_adjoint_memory": (_I32, [_P, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     "amx_probe_fp32_fma": (_I32, [ctypes.POINTER(_D), _P]),
+    "amx_poisson_create": (_I32, [_I32, _I32, _D, _I32, _I32, ctypes.POINTER(_P)]),
+    "amx_poisson_destroy": (_I32, [_P]),
+    "amx_poisson_solve": (_I32, [_P, _P, _P, _D, _P]),
     "amx_version": (ctypes.c_char_p, []),
 }
 
@@ -177,6 +183,7 @@ def make_params(params) -> amx_params:
         minimum_pressure=float(params.minimum_pressure),
         dt_max=float(params.dt_max),
         t_end=float(params.t_end),
+        gravitational_constant=float(getattr(params, "gravitational_constant", 1.0)),
     )
 
 
@@ -390,3 +397,29 @@ def probe_fp32_fma(stream=0) -> float:
     t = ctypes.c_double()
     check(lib().amx_probe_fp32_fma(ctypes.byref(t), _P(stream)), "amx_probe_fp32_fma")
     return t.value
+
+
+class Poisson:
+    """Owns an ``amx_poisson``: the FFT Poisson solve of
+    _compute_gravitational_potential on an n^d grid (periodic, or open via
+    the Hockney-Eastwood zero padding)."""
+
+    def __init__(self, dimensionality, num_cells, grid_spacing, periodic, dtype):
+        self._L = lib()
+        h = _P()
+        check(self._L.amx_poisson_create(int(dimensionality), int(num_cells), float(grid_spacing), int(bool(periodic)),
+                                         int(dtype), ctypes.byref(h)), "amx_poisson_create")
+        self.handle = h
+
+    def solve(self, density_ptr, potential_ptr, G, stream=0):
+        check(self._L.amx_poisson_solve(self.handle, _P(density_ptr), _P(potential_ptr), float(G), _P(stream)),
+              "amx_poisson_solve")
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self._L.amx_poisson_destroy(h)
+            except Exception:
+                pass
+            self.handle = None

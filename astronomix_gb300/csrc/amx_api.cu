@@ -13,6 +13,7 @@
 #include "fd_api.h"
 #include "fv_kernels.cuh"
 #include "fv_registry.h"
+#include "gravity.h"
 
 extern "C" int amx_diag_sums_raw(const amx_config* cfg, const void* state, double gamma, double* out_dev,
                                  void* stream);
@@ -41,6 +42,8 @@ struct amx_plan {
   double* diag = nullptr;   // 8 doubles of reduction scratch for amx_conservation_sums
   // FD
   amx::FDPlan* fd = nullptr;
+  // FV self-gravity (null without)
+  amx::GravPlan* grav = nullptr;
 };
 
 namespace {
@@ -64,6 +67,17 @@ int validate(const amx_config* c) {
     if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA_PP) return AMX_ERR_UNSUPPORTED;
     // the reference's 1D VAN_ALBADA_PP sums its velocity terms over the whole grid
     if (c->limiter == AMX_VAN_ALBADA_PP && !c->split && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
+    if (c->self_gravity) {
+      if (c->self_gravity_version < AMX_SIMPLE_SOURCE_TERM || c->self_gravity_version > AMX_HALF_SPLIT)
+        return AMX_ERR_INVALID_ARG;
+      // the reference sets MINMOD for self-gravity (simulation_config.py:384-389);
+      // the source term reconstructs with any limited-linear limiter, not VAN_ALBADA_PP
+      if (c->limiter == AMX_VAN_ALBADA_PP) return AMX_ERR_UNSUPPORTED;
+      // _self_gravity.py:163-167: the Riemann-split versions are HLLC-only
+      if ((c->self_gravity_version == AMX_RIEMANN_SPLIT || c->self_gravity_version == AMX_RIEMANN_SPLIT_UNSTABLE) &&
+          c->riemann_solver != AMX_HLLC && c->riemann_solver != AMX_HLLC_LM)
+        return AMX_ERR_UNSUPPORTED;
+    }
     if (c->boundary_handling == AMX_GHOST_CELLS) {
       for (int k = 0; k < c->dimensionality; ++k) {
         for (int side = 0; side < 2; ++side) {
@@ -81,6 +95,7 @@ int validate(const amx_config* c) {
   }
   if (c->solver_mode == AMX_FINITE_DIFFERENCE) {
     if (c->dimensionality != 3 || !c->mhd) return AMX_ERR_UNSUPPORTED;
+    if (c->self_gravity) return AMX_ERR_UNSUPPORTED;
     if (c->num_vars != 11) return AMX_ERR_INVALID_ARG;
     if (c->num_cells < 8) return AMX_ERR_INVALID_ARG;
     return AMX_OK;
@@ -173,6 +188,57 @@ int fv_run_mode(amx_plan* p, void* state, const amx_params* prm, int mode, doubl
   return fv_launch(p, a, s);
 }
 
+// A device-driven seam (dt from ctl->dt times dt_scale; skipped unless ctl->active).
+int fv_seam(amx_plan* p, void* state, const amx_params* prm, int mode, double dt_scale, double t_pause,
+            cudaStream_t s) {
+  if (p->cfg.dtype == AMX_F32) {
+    auto a = make_fv_args<float>(p, state, prm, mode);
+    a.dt_dev = 1;
+    a.dt_scale = dt_scale;
+    a.t_pause = t_pause;
+    return fv_launch(p, a, s);
+  }
+  auto a = make_fv_args<double>(p, state, prm, mode);
+  a.dt_dev = 1;
+  a.dt_scale = dt_scale;
+  a.t_pause = t_pause;
+  return fv_launch(p, a, s);
+}
+
+// One step with self-gravity (time_integration.py:626-690 with
+// evolve_state.py:178-322, 429-487 and 497-600): the gravitational source
+// term needs the potential of the density before each gas update, a cuFFT
+// solve between two phases of the persistent kernel, so a step is a
+// stream-ordered sequence of launches with dt, t and the decision to step
+// kept on the device: dt (FV_MODE_DT), per gas update a copy of the gas rows,
+// the hydro seam and the source term, the magnetic seam between the two
+// half updates with MHD, and the time advance.  `evolve_only`: one
+// _evolve_state_fv with the dt already in ctl->dt (no dt, no advance).
+int fv_gravity_step(amx_plan* p, void* state, const amx_params* prm, double t_pause, bool evolve_only,
+                    cudaStream_t s) {
+  const size_t gas_bytes = (size_t)(p->cfg.dimensionality + 2) * (size_t)p->ncells * p->elem;
+  void* old = amx::grav_old_state(p->grav);
+  const double h = p->cfg.mhd ? 0.5 : 1.0;
+  int rc = AMX_OK;
+  if (!evolve_only) {
+    rc = fv_seam(p, state, prm, amx::FV_MODE_DT, 1.0, t_pause, s);
+    if (rc) return rc;
+  }
+  rc |= cuda_ok(cudaMemcpyAsync(old, state, gas_bytes, cudaMemcpyDeviceToDevice, s));
+  rc |= fv_seam(p, state, prm, amx::FV_MODE_HYDRO_RK2, h, INFINITY, s);
+  rc |= amx::grav_apply(p->grav, old, state, p->ctl, h, *prm, s);
+  if (rc) return rc;
+  if (p->cfg.mhd) {
+    rc |= fv_seam(p, state, prm, amx::FV_MODE_MAGNETIC, 1.0, INFINITY, s);
+    rc |= cuda_ok(cudaMemcpyAsync(old, state, gas_bytes, cudaMemcpyDeviceToDevice, s));
+    rc |= fv_seam(p, state, prm, amx::FV_MODE_HYDRO_RK2, h, INFINITY, s);
+    rc |= amx::grav_apply(p->grav, old, state, p->ctl, h, *prm, s);
+    if (rc) return rc;
+  }
+  if (!evolve_only) rc = amx::grav_advance(p->ctl, p->dt_hist, p->it_hist, p->max_hist, p->cfg.mhd, s);
+  return rc;
+}
+
 }  // namespace
 
 // ====================================================================== ABI
@@ -253,6 +319,10 @@ int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out) 
   p->max_hist = max_history;
   p->dt_hist = max_history ? reinterpret_cast<double*>(p->ws + o_dth) : nullptr;
   p->it_hist = max_history ? reinterpret_cast<int*>(p->ws + o_ith) : nullptr;
+  if (cfg->self_gravity) {
+    rc = amx::grav_plan_create(*cfg, &p->grav);
+    if (rc) { amx_plan_destroy(p); return rc; }
+  }
   if (cudaDeviceSynchronize() != cudaSuccess) { amx_plan_destroy(p); return AMX_ERR_CUDA; }
   *out = p;
   return AMX_OK;
@@ -262,6 +332,7 @@ int amx_plan_destroy(amx_plan* p) {
   if (!p) return AMX_OK;
   if (p->diag) cudaFree(p->diag);
   if (p->fd) amx::fd_plan_destroy(p->fd);
+  if (p->grav) amx::grav_plan_destroy(p->grav);
   if (p->ws) cudaFree(p->ws);
   delete p;
   return AMX_OK;
@@ -269,7 +340,7 @@ int amx_plan_destroy(amx_plan* p) {
 
 int amx_plan_workspace_bytes(const amx_plan* p, size_t* bytes) {
   if (!p || !bytes) return AMX_ERR_INVALID_ARG;
-  *bytes = p->fd ? amx::fd_workspace_bytes(p->fd) : p->ws_bytes;
+  *bytes = p->fd ? amx::fd_workspace_bytes(p->fd) : p->ws_bytes + amx::grav_plan_bytes(p->grav);
   return AMX_OK;
 }
 
@@ -301,6 +372,21 @@ int amx_cfl_dt(amx_plan* p, const void* state, const amx_params* prm, double* dt
 
 int amx_fv_hydro_rk2(amx_plan* p, void* state, const amx_params* prm, double dt, void* stream) {
   if (!p || !state || !prm || p->fd) return AMX_ERR_INVALID_ARG;
+  if (p->grav) {
+    // the gas update followed by the gravitational source term (evolve_state.py:429-487)
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int one = 1;
+    const size_t gas_bytes = (size_t)(p->cfg.dimensionality + 2) * (size_t)p->ncells * p->elem;
+    void* old = amx::grav_old_state(p->grav);
+    int rc = cuda_ok(cudaMemcpyAsync(&p->ctl->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, s));
+    rc |= cuda_ok(cudaMemcpyAsync(&p->ctl->active, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    rc |= cuda_ok(cudaStreamSynchronize(s));
+    rc |= cuda_ok(cudaMemcpyAsync(old, state, gas_bytes, cudaMemcpyDeviceToDevice, s));
+    if (rc) return rc;
+    rc = fv_seam(p, state, prm, amx::FV_MODE_HYDRO_RK2, 1.0, INFINITY, s);
+    if (rc) return rc;
+    return amx::grav_apply(p->grav, old, state, p->ctl, 1.0, *prm, s);
+  }
   return fv_run_mode(p, state, prm, amx::FV_MODE_HYDRO_RK2, dt, 1.0, 0, false, static_cast<cudaStream_t>(stream));
 }
 
@@ -314,6 +400,14 @@ int amx_evolve_state(amx_plan* p, void* state, const amx_params* prm, double dt,
   if (!p || !state || !prm) return AMX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (p->fd) return amx::fd_evolve(p->fd, state, *prm, dt, s);
+  if (p->grav) {
+    const int one = 1;
+    int rc = cuda_ok(cudaMemcpyAsync(&p->ctl->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, s));
+    rc |= cuda_ok(cudaMemcpyAsync(&p->ctl->active, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    rc |= cuda_ok(cudaStreamSynchronize(s));
+    if (rc) return rc;
+    return fv_gravity_step(p, state, prm, INFINITY, true, s);
+  }
   return fv_run_mode(p, state, prm, amx::FV_MODE_EVOLVE, dt, 1.0, 0, false, s);
 }
 
@@ -343,6 +437,15 @@ int amx_run_async(amx_plan* p, void* state, const amx_params* prm, int64_t max_s
   if (!p || !state || !prm || max_steps < 0) return AMX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (p->fd) return amx::fd_run(p->fd, state, *prm, max_steps, INFINITY, s);
+  if (p->grav) {
+    // a step is a sequence of launches: queue max_steps of them (bounded)
+    if (max_steps > (1 << 20)) return AMX_ERR_TOO_LARGE;
+    for (int64_t i = 0; i < max_steps; ++i) {
+      const int rc = fv_gravity_step(p, state, prm, INFINITY, false, s);
+      if (rc) return rc;
+    }
+    return AMX_OK;
+  }
   return fv_run_steps(p, state, prm, max_steps, s);
 }
 
@@ -374,6 +477,31 @@ int amx_run_until(amx_plan* p, void* state, const amx_params* prm, int64_t max_s
     if (rc) return rc;
     amx_run_info tmp;
     return read_info(p, info ? info : &tmp, s);
+  }
+  if (p->grav) {
+    // device-driven steps, the host checks t after 1, 2, 4, .. 32 steps
+    int64_t done = 0, chunk = 1;
+    amx_run_info g{};
+    while (done < max_steps) {
+      const int64_t k = std::min<int64_t>(chunk, max_steps - done);
+      for (int64_t i = 0; i < k; ++i) {
+        const int rc = fv_gravity_step(p, state, prm, t_pause, false, s);
+        if (rc) return rc;
+      }
+      done += k;
+      const int rc = read_info(p, &g, s);
+      if (rc) return rc;
+      if (!p->cfg.fixed_timestep && !(g.t < prm->t_end)) break;
+      if (g.t >= t_pause) break;
+      if (g.status & (AMX_ERR_TIMEOUT | AMX_ERR_NAN)) break;
+      chunk = std::min<int64_t>(chunk * 2, 32);
+    }
+    if (max_steps == 0) {
+      const int rc = read_info(p, &g, s);
+      if (rc) return rc;
+    }
+    if (info) *info = g;
+    return AMX_OK;
   }
   // FV: the history records are indexed from the first step of this call
   int rc = AMX_OK;

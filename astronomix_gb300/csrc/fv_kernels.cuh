@@ -41,6 +41,11 @@ struct FVControl {
   unsigned int bar_count, bar_gen;
   int abort_flag;
   int status;
+  // device-driven seams (dt_dev): FV_MODE_DT sets dt and whether a step is
+  // taken; the hydro seam records the maxima of |u_a| + c of its input state
+  int active;
+  int pad1;
+  double seam_maxima[3];
 };
 
 enum FVScheme { FV_UNSPLIT = 0, FV_SPLIT = 1, FV_UNSPLIT_PP = 2 };
@@ -51,6 +56,7 @@ enum FVMode {
   FV_MODE_HYDRO_RK2 = 2,  // one RK2 update of the gas rows with dt_in * dt_scale
   FV_MODE_MAGNETIC = 3,   // one magnetic sub-step with dt_in
   FV_MODE_EVOLVE = 4,     // one _evolve_state_fv with dt_in (no CFL, no t update)
+  FV_MODE_DT = 5,         // dt of the next step into ctl->dt, ctl->active = whether it is taken
 };
 
 template <typename T>
@@ -81,6 +87,7 @@ struct FVArgs {
   double dt_fixed;   // t_end / num_timesteps (fixed mode)
   double dt_in;      // seam modes
   double dt_scale;   // seam modes
+  int dt_dev;        // seam modes: dt from ctl->dt (times dt_scale), nothing done unless ctl->active
   double tol;        // fixed-point tolerance
   int max_iters;     // fixed-point cap (1000 in the reference)
   int mhd;           // the state carries B (the magnetic split is active)
@@ -1270,15 +1277,52 @@ fv_run_kernel(FVArgs<T> a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->dt = dt;
     return;
   }
+  // The dt of the next step of a device-driven step sequence (the step loop
+  // of time_integration.py:626-677): no step once t reached t_end (adaptive
+  // dt), t_pause or an error; otherwise the CFL dt (or the fixed one),
+  // clipped to the end time.  Every block reads the same t and status.
+  if (a.mode == FV_MODE_DT) {
+    const double t = *(volatile double*)&ctl->t;
+    const int st = *(volatile int*)status;
+    bool go = !(t >= a.t_pause) && !(st & (AMX_ERR_TIMEOUT | AMX_ERR_NAN));
+    if (!a.fixed_timestep && !(t < a.t_end)) go = false;
+    if (!go) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) ctl->active = 0;
+      return;
+    }
+    if (!cfl_phase()) return;
+    double dt = a.fixed_timestep ? a.dt_fixed : dt_from_maxima();
+    if (a.exact_end_time) dt = fmin(dt, a.t_end - t);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      ctl->dt = dt;
+      ctl->active = 1;
+    }
+    return;
+  }
   // the seams need the maxima of the state they start from (Lax-Friedrichs alpha)
   if (a.mode == FV_MODE_HYDRO_RK2) {
+    double dt_in = a.dt_in;
+    if (a.dt_dev) {
+      if (!*(volatile int*)&ctl->active) return;
+      dt_in = *(volatile double*)&ctl->dt;
+    }
     if (!cfl_phase()) return;
-    rk2(T(a.dt_in * a.dt_scale), false);
+    if (a.dt_dev && blockIdx.x == 0 && threadIdx.x == 0) {
+      double m[3];
+      last_maxima(m);
+      for (int k = 0; k < 3; ++k) ctl->seam_maxima[k] = m[k];
+    }
+    rk2(T(dt_in * a.dt_scale), false);
     return;
   }
   if (a.mode == FV_MODE_MAGNETIC) {
     if (!MHD) return;
-    const int it = magnetic(T(a.dt_in));
+    double dt_in = a.dt_in;
+    if (a.dt_dev) {
+      if (!*(volatile int*)&ctl->active) return;
+      dt_in = *(volatile double*)&ctl->dt;
+    }
+    const int it = magnetic(T(dt_in));
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->mag_iters = it;
     return;
   }

@@ -46,8 +46,8 @@ class StateStruct(NamedTuple):
 def _check_supported(config: SimulationConfig):
     if config.geometry != CARTESIAN:
         raise NotImplementedError("only Cartesian geometry is part of the accelerated path")
-    if config.self_gravity:
-        raise NotImplementedError("self-gravity is not part of the accelerated MHD step")
+    if config.self_gravity and config.solver_mode != FINITE_VOLUME:
+        raise NotImplementedError("self-gravity is part of the finite-volume scheme only")
     if config.wind_config.stellar_wind or config.cooling_config.cooling or \
             config.cosmic_ray_config.cosmic_rays or config.neural_net_force_config.neural_net_force or \
             config.cnn_mhd_corrector_config.cnn_mhd_corrector or \
@@ -110,6 +110,8 @@ def make_amx_config(config: SimulationConfig, rv: RegisteredVariables, shape, dt
     c.split = int(config.split)
     c.first_order_fallback = int(bool(config.first_order_fallback))
     c.use_max_adaptive_timestep = int(bool(config.use_max_adaptive_timestep))
+    c.self_gravity = int(bool(config.self_gravity))
+    c.self_gravity_version = int(config.self_gravity_version)
     return c
 
 
@@ -191,7 +193,7 @@ def time_integration(primitive_state, config: SimulationConfig, params: Simulati
     n = int(config.num_snapshots)
     ss = config.snapshot_settings
     rec = {"times": [], "states": [], "mass": [], "energy": [], "internal": [], "kinetic": [], "divb": [],
-           "radial": []}
+           "radial": [], "grav": []}
 
     def take(t):
         if config.return_snapshots:
@@ -206,6 +208,11 @@ def time_integration(primitive_state, config: SimulationConfig, params: Simulati
             rec["kinetic"].append(sums[2])
             rec["internal"].append(sums[3])
             rec["divb"].append(sums[4])
+            if config.self_gravity:
+                # calculate_total_energy adds 0.5 rho phi (total_quantities.py:141-145)
+                eg = _gravitational_energy(dev, config, registered_variables, params, stream)
+                rec["energy"][-1] += eg
+                rec["grav"].append(eg)
             if ss.return_radial_momentum:
                 rec["radial"].append(_radial_momentum(dev, config, registered_variables))
         if config.activate_snapshot_callback and snapshot_callable is not None:
@@ -279,6 +286,7 @@ def time_integration(primitive_state, config: SimulationConfig, params: Simulati
         internal_energy=pad(rec["internal"]) if ss.return_internal_energy else None,
         kinetic_energy=pad(rec["kinetic"]) if ss.return_kinetic_energy else None,
         radial_momentum=pad(rec["radial"]) if ss.return_radial_momentum else None,
+        gravitational_energy=pad(rec["grav"]) if (ss.return_gravitational_energy and config.self_gravity) else None,
         magnetic_divergence=pad(rec["divb"]) if (ss.return_magnetic_divergence and config.mhd) else None,
         num_iterations=int(steps_taken),
         current_checkpoint=min(len(rec["times"]), n),
@@ -299,6 +307,47 @@ def _radial_momentum(dev, config, rv):
     rho = dev[rv.density_index].double()
     ur = sum(dev[1 + i].double() * grids[i] for i in range(d)) / r
     return float((rho * ur).sum() * (dx ** d if d > 1 else dx))
+
+
+_POISSON = {}
+
+
+def _poisson(config, n, torch_dtype):
+    """The cached Poisson solver of an n^d grid of this config (periodic when
+    every boundary is, _poisson_solver.py:39-79)."""
+    import torch
+
+    d = int(config.dimensionality)
+    lo, hi = _bc_codes(config)
+    periodic = all(lo[k] == PERIODIC_BOUNDARY and hi[k] == PERIODIC_BOUNDARY for k in range(d))
+    dtype = _native.AMX_F64 if torch_dtype == torch.float64 else _native.AMX_F32
+    key = (d, int(n), float(config.grid_spacing), periodic, dtype)
+    solver = _POISSON.get(key)
+    if solver is None:
+        solver = _native.Poisson(d, n, config.grid_spacing, periodic, dtype)
+        _POISSON[key] = solver
+    return solver
+
+
+def gravitational_potential(density, config, G=1.0):
+    """_compute_gravitational_potential (_poisson_solver.py:17-151) of a CUDA
+    tensor of n^d cells on its own grid, on the device."""
+    import torch
+
+    rho = density.contiguous()
+    phi = torch.empty_like(rho)
+    _poisson(config, rho.shape[-1], rho.dtype).solve(rho.data_ptr(), phi.data_ptr(), float(G), _stream())
+    return phi
+
+
+def _gravitational_energy(dev, config, rv, params, stream):
+    """calculate_gravitational_energy (total_quantities.py:90-104, Cartesian):
+    sum of 0.5 rho phi dx^d, FP64 sum on the device."""
+    d = int(config.dimensionality)
+    rho = dev[rv.density_index]
+    phi = gravitational_potential(rho, config, params.gravitational_constant)
+    e = (0.5 * rho.double() * phi.double()).sum()
+    return float(e * (config.grid_spacing if d == 1 else config.grid_spacing ** d))
 
 
 def _raise_status(status, config):

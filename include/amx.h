@@ -67,6 +67,13 @@ extern "C" {
 #define AMX_IMPLICIT_MIDPOINT 0
 #define AMX_IMPLICIT_EULER 1
 
+/* self-gravity source-term versions (simulation_config.py, self_gravity_version) */
+#define AMX_SIMPLE_SOURCE_TERM 0
+#define AMX_DONOR_ACCOUNTING 1
+#define AMX_RIEMANN_SPLIT 2
+#define AMX_RIEMANN_SPLIT_UNSTABLE 3
+#define AMX_HALF_SPLIT 4
+
 /* Static configuration: the fields of SimulationConfig that select kernels
  * (astronomix/option_classes/simulation_config.py:160-342). */
 typedef struct amx_config {
@@ -92,6 +99,8 @@ typedef struct amx_config {
   int32_t split;                  /* FV: 0 unsplit (SSP-RK2), 1 split (MUSCL-Hancock sweeps) */
   int32_t first_order_fallback;   /* split: piecewise-constant interface states */
   int32_t use_max_adaptive_timestep; /* split: dt = min(dt, dt_max)            */
+  int32_t self_gravity;           /* FV: 0 / 1, the source term after every gas update */
+  int32_t self_gravity_version;   /* AMX_SIMPLE_SOURCE_TERM .. AMX_HALF_SPLIT  */
   int32_t reserved;
 } amx_config;
 
@@ -103,6 +112,7 @@ typedef struct amx_params {
   double minimum_pressure;
   double dt_max;
   double t_end;
+  double gravitational_constant;  /* self-gravity G                        */
 } amx_params;
 
 /* Result of a time-integration call. */
@@ -143,7 +153,9 @@ int amx_cfl_dt(amx_plan* plan, const void* state, const amx_params* prm, double*
 
 /* Replaces _evolve_gas_state_unsplit (one SSP-RK2 update of the gas rows),
  * astronomix/_finite_volume/_state_evolution/evolve_state.py:419-488, with
- * time step dt.  `state` holds the full state; only gas rows change. */
+ * time step dt (with split = 1 the Strang sweeps of _evolve_gas_state_split,
+ * :167-336; with self_gravity followed by the gravitational source term).
+ * `state` holds the full state; only gas rows change. */
 int amx_fv_hydro_rk2(amx_plan* plan, void* state, const amx_params* prm, double dt, void* stream);
 
 /* Replaces magnetic_update,
@@ -164,7 +176,11 @@ int amx_evolve_state(amx_plan* plan, void* state, const amx_params* prm, double 
  * astronomix/time_stepping/time_integration.py:386-801 (adaptive dt with
  * exact end time, or the fixed-step loop): advances `state` in place until
  * t >= prm->t_end or `max_steps` more steps were taken, without a host round
- * trip per step.  Synchronises the stream and fills *info when non-null. */
+ * trip per step.  Synchronises the stream and fills *info when non-null.
+ * With self_gravity a step is a stream-ordered sequence of launches (the
+ * Poisson solve sits between the persistent kernel's phases) with dt, t and
+ * the decision to step on the device; the host checks t after 1, 2, 4 ..
+ * 32 steps. */
 int amx_run(amx_plan* plan, void* state, const amx_params* prm, int64_t max_steps,
             amx_run_info* info, void* stream);
 
@@ -175,7 +191,8 @@ int amx_run_until(amx_plan* plan, void* state, const amx_params* prm, int64_t ma
 
 /* Like amx_run but does not synchronise: launches exactly the work of
  * `max_steps` steps (steps after t_end are skipped on the device).  For
- * timing and for callers that overlap host work. */
+ * timing and for callers that overlap host work.  With self_gravity at most
+ * 2^20 steps per call (AMX_ERR_TOO_LARGE above). */
 int amx_run_async(amx_plan* plan, void* state, const amx_params* prm, int64_t max_steps,
                   void* stream);
 
@@ -294,6 +311,24 @@ int amx_adjoint_uses_stored_tape(const amx_adjoint* adj, int32_t* yes);
 int amx_adjoint_schedule(amx_adjoint* adj, double* dt_host, int32_t* iters_host, int64_t n, int64_t* steps);
 /* Device bytes held for checkpoints and for the tape and cotangents. */
 int amx_adjoint_memory(const amx_adjoint* adj, size_t* checkpoint_bytes, size_t* tape_bytes);
+
+/* ---- self-gravity: the Poisson solve -------------------------------------
+ *
+ * Replaces _compute_gravitational_potential
+ * (astronomix/_physics_modules/_self_gravity/_poisson_solver.py:17-151):
+ * with `periodic` the FFT solve of lap(phi) = 4 pi G (rho - mean(rho)) with
+ * the reference's Green's function (-4 pi G / k^2, -1 / (4 pi) at k = 0);
+ * otherwise the Hockney-Eastwood convolution with the isolated kernel
+ * (-2 pi G r, -2 G log r, -G / r; r = 0 replaced by dx) on the grid padded
+ * to twice its size, scaled by dx^d.  cuFFT transforms (R2C / C2R) on the
+ * device.  Runs with amx_config.self_gravity use the same solver on the
+ * grid the reference solves on (the padded grid with ghost-cell handling). */
+typedef struct amx_poisson amx_poisson;
+int amx_poisson_create(int32_t dimensionality, int32_t num_cells, double grid_spacing, int32_t periodic,
+                       int32_t dtype, amx_poisson** out);
+int amx_poisson_destroy(amx_poisson* solver);
+/* density, potential: device arrays of num_cells^d values (C order). */
+int amx_poisson_solve(amx_poisson* solver, const void* density, void* potential, double G, void* stream);
 
 /* ---- measurement ---------------------------------------------------------- */
 

@@ -44,7 +44,8 @@ def evolve(P, dt, config, params, rv, stats=None):
     gamma = xp.scalar(params.gamma, P)
     if config.solver_mode == FINITE_VOLUME:
         dt_ = xp.scalar(dt, P)
-        return _fv.evolve_state_fv(P, dt_, gamma, config, rv, stats=stats, C_cfl=xp.scalar(params.C_cfl, P))
+        return _fv.evolve_state_fv(P, dt_, gamma, config, rv, stats=stats, C_cfl=xp.scalar(params.C_cfl, P),
+                                   G=params.gravitational_constant)
     return _fd.evolve_state_fd(P, dt, gamma, config.grid_spacing, params.minimum_density,
                                params.minimum_pressure, config.enforce_positivity)
 

@@ -567,10 +567,19 @@ def evolve_gas_split(P, dt, gamma, config, rv):
     return evolve_along_axis(P, dt / 2, gamma, config, rv, 1)
 
 
-def evolve_gas(P, dt, gamma, config, rv, C_cfl=None):
+def evolve_gas(P, dt, gamma, config, rv, C_cfl=None, G=1.0):
+    """The gas update of the configured scheme; with self-gravity, followed by
+    the source term of the potential of the density it started from
+    (evolve_state.py:178-322, 429-487)."""
+    P_old = P
     if config.split == UNSPLIT:
-        return evolve_gas_unsplit(P, dt, gamma, config, rv, C_cfl)
-    return evolve_gas_split(P, dt, gamma, config, rv)
+        P = evolve_gas_unsplit(P, dt, gamma, config, rv, C_cfl)
+    else:
+        P = evolve_gas_split(P, dt, gamma, config, rv)
+    if getattr(config, "self_gravity", False):
+        from .gravity import apply_self_gravity
+        P = apply_self_gravity(P, P_old, config, rv, gamma, G, dt)
+    return P
 
 
 # ----------------------------------------------- magnetic sub-step (Pang-Wu)
@@ -704,21 +713,21 @@ def magnetic_update(B, gas, dx, dt, config, rv, return_iterations=False):
     return Bn, gas
 
 
-def evolve_state_fv(P, dt, gamma, config, rv, stats=None, C_cfl=None):
+def evolve_state_fv(P, dt, gamma, config, rv, stats=None, C_cfl=None, G=1.0):
     """evolve_state.py:497-600 (unsplit or split gas scheme; MHD via the Pang-Wu split).
-    C_cfl is needed by the VAN_ALBADA_PP reconstruction only."""
+    C_cfl is needed by the VAN_ALBADA_PP reconstruction only, G by self-gravity."""
     if not config.mhd:
-        return evolve_gas(P, dt, gamma, config, rv, C_cfl)
+        return evolve_gas(P, dt, gamma, config, rv, C_cfl, G)
     if config.dimensionality < 2:
         raise ValueError("MHD currently not supported in 1D.")
     rv_gas = rv._replace(num_vars=rv.num_vars - 3)
     gas = P[:-3]
     B = P[-3:]
-    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas, C_cfl)
+    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas, C_cfl, G)
     B, gas, it = magnetic_update(B, gas, config.grid_spacing, dt, config, rv, return_iterations=True)
     if stats is not None:
         stats.append(it)
-    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas, C_cfl)
+    gas = evolve_gas(gas, dt / 2, gamma, config, rv_gas, C_cfl, G)
     return xp.concatenate([gas, B], axis=0)
 
 
