@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-arena", action="store_true", help="skip the 256^3 blast comparison")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-run batched ensemble")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 128^3 adjoint workload")
+    ap.add_argument("--no-gravity", action="store_true", help="skip the self-gravity collapse workload")
     ap.add_argument("--case", default=None, choices=["fd", "fv3d", "ensemble", "adjoint"],
                     help="run one small case of a secondary workload and exit (for profilers)")
     return ap.parse_args()
@@ -348,6 +349,63 @@ def time_ensemble(num_runs=64, sequential=True):
         out["sequential_single_run_seconds"] = seq_s
         out["speedup_vs_sequential"] = seq_s / sec
     del work, dev
+    return out
+
+
+def time_gravity(n=128, steps=20, warmup=3, cpu_n=16):
+    """Self-gravity: Evrard's collapse at n^3 (FP32), `steps` steps of the
+    device-driven step sequence timed with CUDA events after `warmup` steps;
+    the open-boundary Poisson solve on the padded grid ((n + 4)^3, zero
+    padded to (2n + 8)^3) timed alone; the oracle on cpu_n^3 for one step on
+    one host core."""
+    import torch
+    from astronomix_gb300 import _native
+    from astronomix_gb300.time_integration import get_plan, gravitational_potential
+    from astronomix_gb300.initial_conditions import evrard_collapse
+
+    cfg, prm, rv, s = evrard_collapse(n)
+    plan = get_plan(cfg, rv, s.shape, np.float32)
+    dev = torch.from_numpy(s).cuda()
+    stream = torch.cuda.current_stream()
+    st = stream.cuda_stream
+    p = _native.make_params(prm)
+    plan.reset(st)
+    info = plan.run(dev.data_ptr(), p, warmup, st)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    plan.run_async(dev.data_ptr(), p, steps, st)
+    b.record(stream)
+    torch.cuda.synchronize()
+    sec = a.elapsed_time(b) / 1e3
+    status = plan.status(stream=st)
+    # the Poisson solve of one gas update, alone (same grid as the run's)
+    m = n + 4
+    rho = torch.rand((m, m, m), device="cuda", dtype=torch.float32) + 0.5
+    for _ in range(3):
+        gravitational_potential(rho, cfg._replace(num_cells=m), 1.0)
+    torch.cuda.synchronize()
+    a.record(stream)
+    reps = 20
+    for _ in range(reps):
+        gravitational_potential(rho, cfg._replace(num_cells=m), 1.0)
+    b.record(stream)
+    torch.cuda.synchronize()
+    poisson_ms = a.elapsed_time(b) / reps
+    out = {"workload": "Evrard collapse %d^3, split MUSCL-Hancock HLLC, RIEMANN_SPLIT_UNSTABLE, reflective walls "
+                       "(open Poisson solve, Hockney-Eastwood)" % n,
+           "steps": steps, "ms_per_step": 1e3 * sec / steps, "zone_updates_per_s": n ** 3 * steps / sec,
+           "poisson_solve_ms": poisson_ms, "poisson_grid": [2 * m] * 3,
+           "poisson_share_of_step": poisson_ms / (1e3 * sec / steps), "status": int(status)}
+    # the oracle (reference algorithm, NumPy) on a small grid, one step
+    from oracle import driver as odriver
+
+    cfg_c, prm_c, rv_c, s_c = evrard_collapse(cpu_n, dtype=np.float64)
+    t0 = time.perf_counter()
+    odriver.time_integration(s_c, cfg_c, prm_c, rv_c, max_steps=1)
+    cpu_s = time.perf_counter() - t0
+    out["cpu_oracle"] = {"grid": [cpu_n] * 3, "zone_updates_per_s": cpu_n ** 3 / cpu_s, "cores": 1}
+    del dev
     return out
 
 
@@ -683,6 +741,7 @@ def run_ours(args, rank, world):
                  "fd_blast_fp32_vs_fp64": fd_precision()}
     ensemble = None if args.no_ensemble else time_ensemble()
     adjoint = None if args.no_adjoint else time_adjoint()
+    gravity = None if args.no_gravity else time_gravity()
 
     if rank != 0:
         return
@@ -724,6 +783,7 @@ def run_ours(args, rank, world):
         "reference_published_workloads": arena,
         "ensemble_fp32": ensemble,
         "adjoint_fp32": adjoint,
+        "self_gravity_fp32": gravity,
         "status": status,
     }
     print(json.dumps(line))
