@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-run batched ensemble")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 128^3 adjoint workload")
     ap.add_argument("--no-gravity", action="store_true", help="skip the self-gravity collapse workload")
-    ap.add_argument("--case", default=None, choices=["fd", "fv3d", "ensemble", "adjoint"],
+    ap.add_argument("--case", default=None, choices=["fd", "fv3d", "ensemble", "adjoint", "gravity"],
                     help="run one small case of a secondary workload and exit (for profilers)")
     return ap.parse_args()
 
@@ -63,7 +63,8 @@ def run_case(name):
     runs (128^2..512^2, t_end / 8) in one batched launch; adjoint: the 3D
     density-perturbation problem at 96^3 to t = 0.01, forward and backward
     with the stored tape (a 4 GB tape budget: the case holds a few GB at
-    most)."""
+    most); gravity: Evrard's collapse at 128^3 FP32, 3 steps of the
+    self-gravity step sequence."""
     import torch
     from astronomix_gb300 import _native
 
@@ -76,6 +77,17 @@ def run_case(name):
         st = torch.cuda.current_stream().cuda_stream
         plan.reset(st)
         info = plan.run(dev.data_ptr(), _native.make_params(prm), 2, st)
+        print(json.dumps({"case": name, "steps": info.steps, "status": info.status}))
+    elif name == "gravity":
+        from astronomix_gb300.time_integration import get_plan
+        from astronomix_gb300.initial_conditions import evrard_collapse
+
+        cfg, prm, rv, s = evrard_collapse(128)
+        plan = get_plan(cfg, rv, s.shape, np.float32)
+        dev = torch.from_numpy(s).cuda()
+        st = torch.cuda.current_stream().cuda_stream
+        plan.reset(st)
+        info = plan.run(dev.data_ptr(), _native.make_params(prm), 3, st)
         print(json.dumps({"case": name, "steps": info.steps, "status": info.status}))
     elif name == "ensemble":
         from astronomix_gb300.ensemble import Ensemble, turbulent_ensemble_member

@@ -227,6 +227,6 @@ def test_evrard_collapse_energy_budget_fp32(cuda):
     m = snap.total_mass
     assert abs(m[-1] - m[0]) < 1e-5 * m[0]
     eg, ek, et = snap.gravitational_energy, snap.kinetic_energy, snap.total_energy
-    assert eg[0] < 0 and ek[0] == 0.0
+    assert eg[0] < 0 and ek[0] < 1e-15  # (|u| carries the reference's 1e-20 under the root)
     assert ek[-1] > 1e-3 * abs(eg[0]) and eg[-1] < eg[0], (eg, ek)
     assert abs(et[-1] - et[0]) < 0.02 * abs(eg[0]), (et, eg, ek)
