@@ -22,24 +22,18 @@
 #include "amx_common.cuh"
 #include "fv_kernels.cuh"
 #include "gravity.h"
+#include "gravity_source.cuh"
+
+namespace amx {
+// instantiated in gravity_f32.cu (approximate FP32 division and square root)
+extern template int grav_source_launch<float>(const GravSrc<float>&, int, int, cudaStream_t);
+}  // namespace amx
 
 namespace amx {
 
 namespace {
 
-constexpr int kGThreads = 256;
 constexpr int kSumBlocks = 304;
-
-// How the FFT grid maps onto the stored cells.
-struct GravGrid {
-  int dim;
-  int n;     // stored cells per axis
-  int goff;  // 2 with ghost-cell handling (the padded grid), 0 otherwise
-  int M;     // n + 2 goff: the grid the reference solves on
-  int E;     // FFT extent per axis: M (periodic) or 2 M (open, zero padded)
-  int roll;  // periodic roll handling: stencil offsets wrap
-  AxisBC bc[3];
-};
 
 template <typename T> struct Cplx;
 template <> struct Cplx<float> { using type = cufftComplex; };
@@ -70,11 +64,7 @@ __device__ __forceinline__ void split_coords(long long e, int ext, int dim, int*
   }
 }
 
-__device__ __forceinline__ long long ext_index(const GravGrid& g, const int* p) {
-  long long r = p[0];
-  for (int k = 1; k < g.dim; ++k) r = r * g.E + p[k];
-  return r;
-}
+__device__ __forceinline__ long long ext_index(const GravGrid& g, const int* p) { return grav_ext_index(g, p); }
 
 __device__ __forceinline__ double block_sum(double v, double* scratch) {
 #pragma unroll
@@ -142,13 +132,12 @@ __global__ void __launch_bounds__(kGThreads) k_density_pack(const T* __restrict_
   }
 }
 
-// Periodic Green's function (_poisson_solver.py:86-113) on the half spectrum,
-// times `scale` (the inverse transform's 1 / E^d): the wave numbers are
-// 2 pi fftfreq(E, dx), -4 pi G / k^2 and -1 / (4 pi) at k = 0.
-template <typename C>
-__global__ void __launch_bounds__(kGThreads) k_green_periodic(C* spec, GravGrid g, double dx, double G, double scale,
-                                                              const int* active) {
-  if (active && !*(volatile const int*)active) return;
+// Periodic Green's function (_poisson_solver.py:86-113) on the half spectrum
+// for G = 1, times `scale` (the inverse transform's 1 / E^d), computed once
+// per solver: the wave numbers are 2 pi fftfreq(E, dx), -4 pi / k^2 and
+// -1 / (4 pi) at k = 0.
+template <typename R>
+__global__ void __launch_bounds__(kGThreads) k_green_periodic_init(R* green, GravGrid g, double dx, double scale) {
   const int E = g.E, H = E / 2 + 1;
   const long long total = ipow_ll(E, g.dim - 1) * H;
   const double val = 1.0 / ((double)E * dx);
@@ -171,8 +160,19 @@ __global__ void __launch_bounds__(kGThreads) k_green_periodic(C* spec, GravGrid 
       k2 = (k == 0) ? kk * kk : k2 + kk * kk;
     }
     if (k2 == 0.0) k2 = 1e-12;
-    const double green = (k2 > 1e-12) ? (-4.0 * pi * G) / k2 : -1.0 / (4.0 * pi);
-    const double f = green * scale;
+    const double gr = (k2 > 1e-12) ? (-4.0 * pi) / k2 : -1.0 / (4.0 * pi);
+    green[e] = R(gr * scale);
+  }
+}
+
+// The spectrum times the real Green's function times G (periodic).
+template <typename C, typename R>
+__global__ void __launch_bounds__(kGThreads) k_spec_scale(C* spec, const R* __restrict__ green, long long total, R G,
+                                                          const int* active) {
+  if (active && !*(volatile const int*)active) return;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const R f = green[e] * G;
     C z = spec[e];
     z.x = z.x * f;
     z.y = z.y * f;
@@ -180,18 +180,18 @@ __global__ void __launch_bounds__(kGThreads) k_green_periodic(C* spec, GravGrid 
   }
 }
 
-// Open boundaries: the spectrum times the isolated kernel's spectrum (G = 1),
-// times G and `scale` (dx^d / E^d).
-template <typename C>
-__global__ void __launch_bounds__(kGThreads) k_green_open(C* spec, const C* __restrict__ kspec, long long total,
-                                                          double f, const int* active) {
+// The spectrum times the isolated kernel's spectrum (G = 1, scaled by
+// dx^d / E^d once per solver) times G (open boundaries).
+template <typename C, typename R>
+__global__ void __launch_bounds__(kGThreads) k_spec_mul(C* spec, const C* __restrict__ kspec, long long total, R G,
+                                                        const int* active) {
   if (active && !*(volatile const int*)active) return;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
     const C a = spec[e], b = kspec[e];
     C z;
-    z.x = (a.x * b.x - a.y * b.y) * f;
-    z.y = (a.x * b.y + a.y * b.x) * f;
+    z.x = (a.x * b.x - a.y * b.y) * G;
+    z.y = (a.x * b.y + a.y * b.x) * G;
     spec[e] = z;
   }
 }
@@ -225,12 +225,12 @@ __global__ void __launch_bounds__(kGThreads) k_open_kernel(double* out, GravGrid
 }
 
 template <typename C, typename D>
-__global__ void k_convert_spectrum(const D* in, C* out, long long total) {
+__global__ void k_convert_spectrum(const D* in, C* out, long long total, double scale) {
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
     C z;
-    z.x = in[e].x;
-    z.y = in[e].y;
+    z.x = in[e].x * scale;
+    z.y = in[e].y * scale;
     out[e] = z;
   }
 }
@@ -244,219 +244,6 @@ __global__ void k_crop(const T* __restrict__ fout, GravGrid g, T* __restrict__ o
     int p[3];
     split_coords(e, g.M, g.dim, p);
     out[e] = fout[ext_index(g, p)];
-  }
-}
-
-// ----------------------------------------------------------- source term
-
-template <typename T>
-struct GravSrc {
-  const T* old;    // gas rows before the gas update
-  T* state;        // gas rows after it (updated in place)
-  const T* phi;    // potential on the FFT grid (solve-grid corner)
-  GravGrid g;
-  long long nc;
-  const FVControl* ctl;
-  double dt_scale;
-  double dx;
-  double gamma;
-  int version;
-  int lm;
-  int split;
-  int first_order;
-  int limiter;
-};
-
-// What each cell accounts for of the mass flux through an interface, for
-// RIEMANN_SPLIT(_UNSTABLE) (_self_gravity.py:159-284): the HLLC dissipation
-// split between the two cells; `to_im1` is the right cell's share, `im1`
-// the left cell's.
-template <typename T, int DIM>
-__device__ __forceinline__ void riemann_split_mass(const T* qL, const T* qR, int d, T gamma, bool lm,
-                                                   bool unstable, T* to_im1, T* im1) {
-  constexpr int P = DIM + 1;
-  const T rhoL = qL[0], uL = qL[d], pL = qL[P];
-  const T rhoR = qR[0], uR = qR[d], pR = qR[P];
-  const T cL = sound_speed(rhoL, pL, gamma), cR = sound_speed(rhoR, pR, gamma);
-  const T FL = uL * rhoL, FR = uR * rhoR;
-  const T sL = Num<T>::sqrt_(rhoL), sR = Num<T>::sqrt_(rhoR);
-  const T u_hat = (sL * uL + sR * uR) / (sL + sR);
-  const T c_hat_sq = (cL * cL * sL + cR * cR * sR) / (sL + sR) +
-                     T(0.5) * (sL * sR / ((sL + sR) * (sL + sR))) * ((uR - uL) * (uR - uL));
-  const T c_hat = Num<T>::sqrt_(c_hat_sq);
-  const T SL = jmin(uL - cL, u_hat - c_hat);
-  const T SR = jmax(uR + cR, u_hat + c_hat);
-  const T S_star = (pR - pL + rhoL * uL * (SL - uL) - rhoR * uR * (SR - uR)) / (rhoL * (SL - uL) - rhoR * (SR - uR));
-  const T USL = rhoL * (SL - uL) / (SL - S_star);
-  const T USR = rhoR * (SR - uR) / (SR - S_star);
-  T SLs = SL, SRs = SR;
-  if (lm) {
-    const T Ma = jmax(Num<T>::abs_(uL / cL), Num<T>::abs_(uR / cR));
-    const T ph = Num<T>::sin_(jmin(T(1), Ma / T(0.1)) * T(3.141592653589793) / T(2));
-    SLs = SL * ph;
-    SRs = SR * ph;
-  }
-  const T diss = T(0.5) * (SLs * (USL - rhoL) + Num<T>::abs_(S_star) * (USL - USR) + SRs * (USR - rhoR));
-  T a = T(0.5) * FR + jmin(diss, T(0));
-  T b = T(0.5) * FL + jmax(diss, T(0));
-  if (unstable) {
-    a = (SR <= T(0)) ? FR / T(2) : a;
-    a = (SL >= T(0)) ? FL / T(2) : a;
-    b = (SL >= T(0)) ? FL / T(2) : b;
-    b = (SR <= T(0)) ? FR / T(2) : b;
-  }
-  *to_im1 = a;
-  *im1 = b;
-}
-
-// _gravitational_source_term_along_axis for every axis and the explicit
-// update of _apply_self_gravity, one cell per thread: the central
-// acceleration -(phi[i+1] - phi[i-1]) / 2dx gives the momentum source rho a;
-// the energy source is rho v a (SIMPLE_SOURCE_TERM) or the mass fluxes
-// through the cell's two interfaces, from the interface states of the old
-// state and the configured Riemann solver, times the one-sided
-// accelerations, shared per version.  U += dt S, back to primitives.
-template <typename T, int DIM, int RS>
-__global__ void __launch_bounds__(kGThreads) k_grav_source(GravSrc<T> a) {
-  constexpr int NV = DIM + 2, P = DIM + 1;
-  const FVControl* ctl = a.ctl;
-  if (!*(volatile const int*)&ctl->active) return;
-  const T h = T(*(volatile const double*)&ctl->dt * a.dt_scale);
-  const T gamma = T(a.gamma);
-  const T dxT = T(a.dx);
-  const T two_dx = T(2.0 * a.dx);
-  const GravGrid g = a.g;
-  const int n = g.n;
-  const long long nc = a.nc;
-  const int version = a.version;
-  const bool lm = a.lm != 0;
-  T alpha[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) alpha[k] = T(((volatile const double*)ctl->seam_maxima)[k]);
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
-    int ic[3] = {0, 0, 0};
-    {
-      long long r = c;
-      for (int k = DIM - 1; k >= 0; --k) {
-        ic[k] = (int)(r % n);
-        r /= n;
-      }
-    }
-    T q0[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) q0[v] = a.old[v * nc + c];
-    const T rho = q0[0];
-    T mS[DIM];
-    T eS = T(0);
-#pragma unroll
-    for (int k = 0; k < DIM; ++k) {
-      // potential at i-1, i, i+1 along k
-      int p[3] = {ic[0] + g.goff, ic[1] + g.goff, ic[2] + g.goff};
-      T ph[3];
-#pragma unroll
-      for (int o = -1; o <= 1; ++o) {
-        int pp[3] = {p[0], p[1], p[2]};
-        pp[k] = g.roll ? wrap(p[k] + o, n) : p[k] + o;
-        ph[o + 1] = a.phi[ext_index(g, pp)];
-      }
-      const T acc = -(ph[2] - ph[0]) / two_dx;
-      mS[k] = rho * acc;
-      T e;
-      if (version == AMX_SIMPLE_SOURCE_TERM) {
-        e = rho * q0[k + 1] * acc;
-      } else {
-        // the old state at i-2 .. i+2 along k (boundary mapped)
-        T q[5][NV];
-#pragma unroll
-        for (int o = -2; o <= 2; ++o) {
-          if (o == 0) {
-#pragma unroll
-            for (int v = 0; v < NV; ++v) q[2][v] = q0[v];
-            continue;
-          }
-          int jc[3] = {ic[0], ic[1], ic[2]};
-          bool flip = false;
-          jc[k] = g.roll ? wrap(ic[k] + o, n) : map_index(ic[k] + o, n, g.bc[k], DIM == 1, &flip);
-          long long cc = jc[0];
-          if (DIM >= 2) cc = cc * n + jc[1];
-          if (DIM >= 3) cc = cc * n + jc[2];
-#pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            T val = a.old[v * nc + cc];
-            if (flip && v == k + 1) val = -val;
-            q[o + 2][v] = val;
-          }
-        }
-        // interface states of the faces i-1/2 (a) and i+1/2 (b)
-        T aL[NV], aR[NV], bL[NV], bR[NV];
-        if (a.first_order) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            aL[v] = q[1][v];
-            aR[v] = q[2][v];
-            bL[v] = q[2][v];
-            bR[v] = q[3][v];
-          }
-        } else if (a.split) {
-          T lo[NV], hi[NV];
-          muscl_states<T, DIM>(q[0], q[1], q[2], k + 1, gamma, h, dxT, a.limiter, lo, hi);
-#pragma unroll
-          for (int v = 0; v < NV; ++v) aL[v] = hi[v];
-          muscl_states<T, DIM>(q[1], q[2], q[3], k + 1, gamma, h, dxT, a.limiter, lo, hi);
-#pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            aR[v] = lo[v];
-            bL[v] = hi[v];
-          }
-          muscl_states<T, DIM>(q[2], q[3], q[4], k + 1, gamma, h, dxT, a.limiter, lo, hi);
-#pragma unroll
-          for (int v = 0; v < NV; ++v) bR[v] = lo[v];
-        } else {
-#pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            const T dm = limited((q[1][v] - q[0][v]) / dxT, (q[2][v] - q[1][v]) / dxT, a.limiter, dxT) * dxT / T(2);
-            const T d0 = limited((q[2][v] - q[1][v]) / dxT, (q[3][v] - q[2][v]) / dxT, a.limiter, dxT) * dxT / T(2);
-            const T dp = limited((q[3][v] - q[2][v]) / dxT, (q[4][v] - q[3][v]) / dxT, a.limiter, dxT) * dxT / T(2);
-            aL[v] = q[1][v] + dm;
-            aR[v] = q[2][v] - d0;
-            bL[v] = q[2][v] + d0;
-            bR[v] = q[3][v] - dp;
-          }
-        }
-        T f_to_im1, f_to_ip1;
-        if (version == AMX_RIEMANN_SPLIT || version == AMX_RIEMANN_SPLIT_UNSTABLE) {
-          const bool unstable = version == AMX_RIEMANN_SPLIT_UNSTABLE;
-          T x, y;
-          riemann_split_mass<T, DIM>(aL, aR, k + 1, gamma, lm, unstable, &f_to_im1, &x);
-          riemann_split_mass<T, DIM>(bL, bR, k + 1, gamma, lm, unstable, &y, &f_to_ip1);
-        } else {
-          T Fa[NV], Fb[NV];
-          riemann<T, DIM, RS>(aL, aR, k + 1, gamma, alpha[k], lm, Fa);
-          riemann<T, DIM, RS>(bL, bR, k + 1, gamma, alpha[k], lm, Fb);
-          if (version == AMX_DONOR_ACCOUNTING) {
-            f_to_ip1 = jmax(Fb[0], T(0));
-            f_to_im1 = jmin(Fa[0], T(0));
-          } else {  // HALF_SPLIT
-            f_to_ip1 = T(0.5) * Fb[0];
-            f_to_im1 = T(0.5) * Fa[0];
-          }
-        }
-        const T acc_b = -(ph[1] - ph[0]) / dxT;
-        const T acc_f = -(ph[2] - ph[1]) / dxT;
-        e = f_to_im1 * acc_b + f_to_ip1 * acc_f;
-      }
-      eS = (k == 0) ? e : eS + e;
-    }
-    T qn[NV], U[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) qn[v] = a.state[v * nc + c];
-    prim_to_cons<T, DIM>(qn, U, gamma);
-#pragma unroll
-    for (int k = 0; k < DIM; ++k) U[k + 1] = U[k + 1] + h * mS[k];
-    U[P] = U[P] + h * eS;
-    cons_to_prim<T, DIM>(U, qn, gamma);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) a.state[v * nc + c] = qn[v];
   }
 }
 
@@ -476,12 +263,7 @@ __global__ void k_grav_advance(FVControl* ctl, double* dt_hist, int* it_hist, lo
 inline int cuda_ok(cudaError_t e) { return e == cudaSuccess ? AMX_OK : AMX_ERR_CUDA; }
 inline int fft_ok(cufftResult r) { return r == CUFFT_SUCCESS ? AMX_OK : AMX_ERR_CUDA; }
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-int grid_for(long long work, int num_sms) {
-  const long long b = (work + kGThreads - 1) / kGThreads;
-  const long long cap = (long long)num_sms * 8;
-  return (int)(b < 1 ? 1 : (b < cap ? b : cap));
-}
+inline int grid_for(long long work, int num_sms) { return grav_grid_for(work, num_sms); }
 
 }  // namespace
 
@@ -502,8 +284,10 @@ struct GravPlan {
   void* fin = nullptr;    // FFT input (E^d real)
   void* fout = nullptr;   // inverse transform (E^d real): the potential in its solve-grid corner
   void* spec = nullptr;   // half spectrum
-  void* kspec = nullptr;  // open: the isolated kernel's half spectrum
+  void* kspec = nullptr;  // the Green's function's half spectrum for G = 1, with the inverse
+                          // transform's scale: real (periodic) or complex (open)
   void* old = nullptr;    // run: gas rows of the state before a gas update
+  void* eacc = nullptr;   // run: [ncells] energy source summed over the axes
   double* partial = nullptr;
   unsigned int* counter = nullptr;
   double* mean = nullptr;
@@ -531,8 +315,9 @@ int solver_create(const GravGrid& g, double dx, bool periodic, int dtype, int ol
   const size_t o_in = off; off = align256(off + elem * nreal);
   const size_t o_out = off; off = align256(off + elem * nreal);
   const size_t o_sp = off; off = align256(off + 2 * elem * ncplx);
-  const size_t o_ks = off; off = align256(off + (periodic ? 0 : 2 * elem * ncplx));
+  const size_t o_ks = off; off = align256(off + (periodic ? 1 : 2) * elem * ncplx);
   const size_t o_old = off; off = align256(off + elem * (size_t)old_rows * ncells);
+  const size_t o_eacc = off; off = align256(off + (old_rows ? elem * (size_t)ncells : 0));
   const size_t o_part = off; off = align256(off + sizeof(double) * kSumBlocks);
   const size_t o_cnt = off; off = align256(off + sizeof(unsigned int));
   const size_t o_mean = off; off = align256(off + sizeof(double));
@@ -542,8 +327,9 @@ int solver_create(const GravGrid& g, double dx, bool periodic, int dtype, int ol
   p->fin = p->mem + o_in;
   p->fout = p->mem + o_out;
   p->spec = p->mem + o_sp;
-  p->kspec = periodic ? nullptr : p->mem + o_ks;
+  p->kspec = p->mem + o_ks;
   p->old = old_rows ? p->mem + o_old : nullptr;
+  p->eacc = old_rows ? p->mem + o_eacc : nullptr;
   p->partial = reinterpret_cast<double*>(p->mem + o_part);
   p->counter = reinterpret_cast<unsigned int*>(p->mem + o_cnt);
   p->mean = reinterpret_cast<double*>(p->mem + o_mean);
@@ -555,6 +341,16 @@ int solver_create(const GravGrid& g, double dx, bool periodic, int dtype, int ol
     rc = fft_ok(cufftPlanMany(&p->inv, g.dim, nn, nullptr, 1, 0, nullptr, 1, 0,
                               dtype == AMX_F32 ? CUFFT_C2R : CUFFT_Z2D, 1));
     p->have_inv = rc == AMX_OK;
+  }
+  const double inv_total = 1.0 / (double)nreal;
+  if (!rc && periodic) {
+    if (dtype == AMX_F32)
+      k_green_periodic_init<float><<<grid_for(ncplx, p->num_sms), kGThreads>>>(static_cast<float*>(p->kspec), g, dx,
+                                                                               inv_total);
+    else
+      k_green_periodic_init<double><<<grid_for(ncplx, p->num_sms), kGThreads>>>(static_cast<double*>(p->kspec), g,
+                                                                                dx, inv_total);
+    rc = cuda_ok(cudaGetLastError());
   }
   if (!rc && !periodic) {
     // the isolated kernel's spectrum, in FP64 whatever the state precision
@@ -568,11 +364,15 @@ int solver_create(const GravGrid& g, double dx, bool periodic, int dtype, int ol
       k_open_kernel<<<grid_for(nreal, p->num_sms), kGThreads>>>(kr, g, dx);
       rc = fft_ok(cufftExecD2Z(kp, kr, kc));
       if (!rc) {
+        // the reference scales the cropped potential by dx^d (_poisson_solver.py:151)
+        const double scale = std::pow(dx, g.dim) * inv_total;
         if (dtype == AMX_F32)
           k_convert_spectrum<cufftComplex, cufftDoubleComplex>
-              <<<grid_for(ncplx, p->num_sms), kGThreads>>>(kc, static_cast<cufftComplex*>(p->kspec), ncplx);
+              <<<grid_for(ncplx, p->num_sms), kGThreads>>>(kc, static_cast<cufftComplex*>(p->kspec), ncplx, scale);
         else
-          rc = cuda_ok(cudaMemcpy(p->kspec, kc, sizeof(cufftDoubleComplex) * ncplx, cudaMemcpyDeviceToDevice));
+          k_convert_spectrum<cufftDoubleComplex, cufftDoubleComplex>
+              <<<grid_for(ncplx, p->num_sms), kGThreads>>>(kc, static_cast<cufftDoubleComplex*>(p->kspec), ncplx,
+                                                           scale);
       }
       rc |= cuda_ok(cudaDeviceSynchronize());
       cufftDestroy(kp);
@@ -614,15 +414,13 @@ int potential(GravPlan* p, const T* rho, double G, const int* active, cudaStream
     rc = fft_ok(cufftExecD2Z(p->fwd, static_cast<cufftDoubleReal*>(p->fin), static_cast<cufftDoubleComplex*>(p->spec)));
   }
   if (rc) return rc;
-  const double inv_total = 1.0 / (double)nreal;
   const int cgrid = grid_for(ncplx, p->num_sms);
-  if (p->periodic) {
-    k_green_periodic<C><<<cgrid, kGThreads, 0, s>>>(static_cast<C*>(p->spec), g, p->dx, G, inv_total, active);
-  } else {
-    const double f = G * std::pow(p->dx, g.dim) * inv_total;
-    k_green_open<C><<<cgrid, kGThreads, 0, s>>>(static_cast<C*>(p->spec), static_cast<const C*>(p->kspec), ncplx, f,
-                                                active);
-  }
+  if (p->periodic)
+    k_spec_scale<C, T><<<cgrid, kGThreads, 0, s>>>(static_cast<C*>(p->spec), static_cast<const T*>(p->kspec), ncplx,
+                                                   T(G), active);
+  else
+    k_spec_mul<C, T><<<cgrid, kGThreads, 0, s>>>(static_cast<C*>(p->spec), static_cast<const C*>(p->kspec), ncplx,
+                                                 T(G), active);
   rc = cuda_ok(cudaGetLastError());
   if (rc) return rc;
   if (sizeof(T) == 4) {
@@ -633,41 +431,28 @@ int potential(GravPlan* p, const T* rho, double G, const int* active, cudaStream
   return rc;
 }
 
-template <typename T, int DIM>
-int launch_source(GravPlan* p, const T* old, T* state, const FVControl* ctl, double dt_scale, double gamma,
-                  cudaStream_t s) {
-  GravSrc<T> a{};
-  a.old = old;
-  a.state = state;
-  a.phi = static_cast<const T*>(p->fout);
-  a.g = p->g;
-  a.nc = p->ncells;
-  a.ctl = ctl;
-  a.dt_scale = dt_scale;
-  a.dx = p->dx;
-  a.gamma = gamma;
-  a.version = p->version;
-  a.lm = p->lm;
-  a.split = p->split;
-  a.first_order = p->first_order;
-  a.limiter = p->limiter;
-  const int grid = grid_for(p->ncells, p->num_sms);
-  if (p->rs == AMX_LAX_FRIEDRICHS) k_grav_source<T, DIM, RS_LF><<<grid, kGThreads, 0, s>>>(a);
-  else if (p->rs == AMX_HLL) k_grav_source<T, DIM, RS_HLL><<<grid, kGThreads, 0, s>>>(a);
-  else k_grav_source<T, DIM, RS_HLLC><<<grid, kGThreads, 0, s>>>(a);
-  return cuda_ok(cudaGetLastError());
-}
-
 template <typename T>
 int apply_t(GravPlan* p, const T* old, T* state, const FVControl* ctl, double dt_scale, const amx_params& prm,
             cudaStream_t s) {
   int rc = potential<T>(p, old, prm.gravitational_constant, &ctl->active, s);
   if (rc) return rc;
-  switch (p->g.dim) {
-    case 1: return launch_source<T, 1>(p, old, state, ctl, dt_scale, prm.gamma, s);
-    case 2: return launch_source<T, 2>(p, old, state, ctl, dt_scale, prm.gamma, s);
-    default: return launch_source<T, 3>(p, old, state, ctl, dt_scale, prm.gamma, s);
-  }
+  GravSrc<T> a{};
+  a.old = old;
+  a.state = state;
+  a.phi = static_cast<const T*>(p->fout);
+  a.eacc = static_cast<T*>(p->eacc);
+  a.g = p->g;
+  a.nc = p->ncells;
+  a.ctl = ctl;
+  a.dt_scale = dt_scale;
+  a.dx = p->dx;
+  a.gamma = prm.gamma;
+  a.version = p->version;
+  a.lm = p->lm;
+  a.split = p->split;
+  a.first_order = p->first_order;
+  a.limiter = p->limiter;
+  return grav_source_launch<T>(a, p->rs, p->num_sms, s);
 }
 
 bool all_periodic(const amx_config& c) {
