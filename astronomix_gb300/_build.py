@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--ex
 # the slowest units first, so that the parallel build finishes early
 SOURCES = ["fv_f32_schemes.cu", "fv_f64_schemes.cu", "fv_batch_f32.cu", "fv_batch_f32_alt.cu", "adjoint_f32.cu",
            "adjoint_f64.cu", "amx_api.cu", "fv_f32.cu", "fv_f64.cu", "fd.cu", "fd_f32.cu", "fd_f64.cu",
-           "fv_batch_f64.cu", "batch.cu", "adjoint.cu", "gravity.cu", "gravity_f32.cu", "diag.cu"]
+           "fv_batch_f64.cu", "batch.cu", "adjoint.cu", "gravity.cu", "gravity_f32.cu", "forcing.cu", "diag.cu"]
 
 # FP32 FV kernels use approximate division and square root: the FP32 path is
 # held to an L1 tolerance against FP64, while the FP64 units keep IEEE

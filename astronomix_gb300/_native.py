@@ -70,6 +70,9 @@ class amx_config(ctypes.Structure):
         ("use_max_adaptive_timestep", ctypes.c_int32),
         ("self_gravity", ctypes.c_int32),
         ("self_gravity_version", ctypes.c_int32),
+        ("stellar_wind", ctypes.c_int32),
+        ("num_injection_cells", ctypes.c_int32),
+        ("turbulent_forcing", ctypes.c_int32),
         ("reserved", ctypes.c_int32),
     ]
 
@@ -83,6 +86,10 @@ class amx_params(ctypes.Structure):
         ("dt_max", ctypes.c_double),
         ("t_end", ctypes.c_double),
         ("gravitational_constant", ctypes.c_double),
+        ("wind_mass_loss_rate", ctypes.c_double),
+        ("wind_final_velocity", ctypes.c_double),
+        ("energy_injection_rate", ctypes.c_double),
+        ("forcing_seed", ctypes.c_int64),
     ]
 
 
@@ -184,6 +191,11 @@ def make_params(params) -> amx_params:
         dt_max=float(params.dt_max),
         t_end=float(params.t_end),
         gravitational_constant=float(getattr(params, "gravitational_constant", 1.0)),
+        wind_mass_loss_rate=float(params.wind_params.wind_mass_loss_rate) if hasattr(params, "wind_params") else 0.0,
+        wind_final_velocity=float(params.wind_params.wind_final_velocity) if hasattr(params, "wind_params") else 0.0,
+        energy_injection_rate=float(params.turbulent_forcing_params.energy_injection_rate)
+        if hasattr(params, "turbulent_forcing_params") else 0.0,
+        forcing_seed=42,
     )
 
 

@@ -175,7 +175,8 @@ int amx_adjoint_create(const amx_config* cfg, int32_t checkpoint_every, int64_t 
   if (cfg->solver_mode != AMX_FINITE_VOLUME) return AMX_ERR_UNSUPPORTED;
   if (cfg->dimensionality != 2 && cfg->dimensionality != 3) return AMX_ERR_UNSUPPORTED;
   if (cfg->riemann_solver != AMX_HLL || cfg->limiter != AMX_MINMOD) return AMX_ERR_UNSUPPORTED;
-  if (cfg->fixed_timestep || cfg->split || cfg->self_gravity) return AMX_ERR_UNSUPPORTED;
+  if (cfg->fixed_timestep || cfg->split || cfg->self_gravity || cfg->turbulent_forcing || cfg->stellar_wind)
+    return AMX_ERR_UNSUPPORTED;
   const bool roll = cfg->boundary_handling == AMX_PERIODIC_ROLL;
   for (int k = 0; k < cfg->dimensionality && !roll; ++k)
     if (cfg->bc_lo[k] != AMX_BC_PERIODIC || cfg->bc_hi[k] != AMX_BC_PERIODIC) return AMX_ERR_UNSUPPORTED;

@@ -13,6 +13,7 @@
 #include "fd_api.h"
 #include "fv_kernels.cuh"
 #include "fv_registry.h"
+#include "forcing.h"
 #include "gravity.h"
 
 extern "C" int amx_diag_sums_raw(const amx_config* cfg, const void* state, double gamma, double* out_dev,
@@ -42,8 +43,9 @@ struct amx_plan {
   double* diag = nullptr;   // 8 doubles of reduction scratch for amx_conservation_sums
   // FD
   amx::FDPlan* fd = nullptr;
-  // FV self-gravity (null without)
+  // FV self-gravity and turbulent forcing (null without)
   amx::GravPlan* grav = nullptr;
+  amx::ForcingPlan* force = nullptr;
 };
 
 namespace {
@@ -67,6 +69,12 @@ int validate(const amx_config* c) {
     if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA_PP) return AMX_ERR_UNSUPPORTED;
     // the reference's 1D VAN_ALBADA_PP sums its velocity terms over the whole grid
     if (c->limiter == AMX_VAN_ALBADA_PP && !c->split && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
+    // FV wind injection (the physics-module path) is not part of this library
+    if (c->stellar_wind) return AMX_ERR_UNSUPPORTED;
+    // the forcing field has the unpadded grid's shape (_turbulent_forcing.py:30-40):
+    // 3D with periodic roll, as in the reference
+    if (c->turbulent_forcing && (c->dimensionality != 3 || c->boundary_handling != AMX_PERIODIC_ROLL))
+      return AMX_ERR_UNSUPPORTED;
     if (c->self_gravity) {
       if (c->self_gravity_version < AMX_SIMPLE_SOURCE_TERM || c->self_gravity_version > AMX_HALF_SPLIT)
         return AMX_ERR_INVALID_ARG;
@@ -205,36 +213,44 @@ int fv_seam(amx_plan* p, void* state, const amx_params* prm, int mode, double dt
   return fv_launch(p, a, s);
 }
 
-// One step with self-gravity (time_integration.py:626-690 with
-// evolve_state.py:178-322, 429-487 and 497-600): the gravitational source
-// term needs the potential of the density before each gas update, a cuFFT
-// solve between two phases of the persistent kernel, so a step is a
-// stream-ordered sequence of launches with dt, t and the decision to step
-// kept on the device: dt (FV_MODE_DT), per gas update a copy of the gas rows,
-// the hydro seam and the source term, the magnetic seam between the two
-// half updates with MHD, and the time advance.  `evolve_only`: one
-// _evolve_state_fv with the dt already in ctl->dt (no dt, no advance).
-int fv_gravity_step(amx_plan* p, void* state, const amx_params* prm, double t_pause, bool evolve_only,
-                    cudaStream_t s) {
-  const size_t gas_bytes = (size_t)(p->cfg.dimensionality + 2) * (size_t)p->ncells * p->elem;
-  void* old = amx::grav_old_state(p->grav);
-  const double h = p->cfg.mhd ? 0.5 : 1.0;
+// One device-driven step (time_integration.py:626-762) for runs whose step
+// needs work between the persistent kernel's phases: self-gravity (the
+// Poisson solve after each gas update, evolve_state.py:178-322, 429-487) and
+// turbulent forcing (before the evolve, :700-711), both cuFFT-based.  The
+// step is a stream-ordered sequence of launches with dt, t and the decision
+// to step kept on the device: dt (FV_MODE_DT), the forcing, then with
+// gravity per gas update a copy of the gas rows, the hydro seam and the
+// source term (the magnetic seam between the two half updates with MHD),
+// without gravity the evolve seam; and the time advance.  `evolve_only`: one
+// _evolve_state_fv with the dt already in ctl->dt (no dt, no forcing, no
+// advance).
+int fv_device_step(amx_plan* p, void* state, const amx_params* prm, double t_pause, bool evolve_only,
+                   cudaStream_t s) {
   int rc = AMX_OK;
   if (!evolve_only) {
     rc = fv_seam(p, state, prm, amx::FV_MODE_DT, 1.0, t_pause, s);
+    if (!rc && p->force)
+      rc = amx::forcing_apply(p->force, state, &p->ctl->dt, &p->ctl->active, &p->ctl->steps, *prm, s);
     if (rc) return rc;
   }
-  rc |= cuda_ok(cudaMemcpyAsync(old, state, gas_bytes, cudaMemcpyDeviceToDevice, s));
-  rc |= fv_seam(p, state, prm, amx::FV_MODE_HYDRO_RK2, h, INFINITY, s);
-  rc |= amx::grav_apply(p->grav, old, state, p->ctl, h, *prm, s);
-  if (rc) return rc;
-  if (p->cfg.mhd) {
-    rc |= fv_seam(p, state, prm, amx::FV_MODE_MAGNETIC, 1.0, INFINITY, s);
+  if (!p->grav) {
+    rc = fv_seam(p, state, prm, amx::FV_MODE_EVOLVE, 1.0, INFINITY, s);
+  } else {
+    const size_t gas_bytes = (size_t)(p->cfg.dimensionality + 2) * (size_t)p->ncells * p->elem;
+    void* old = amx::grav_old_state(p->grav);
+    const double h = p->cfg.mhd ? 0.5 : 1.0;
     rc |= cuda_ok(cudaMemcpyAsync(old, state, gas_bytes, cudaMemcpyDeviceToDevice, s));
     rc |= fv_seam(p, state, prm, amx::FV_MODE_HYDRO_RK2, h, INFINITY, s);
     rc |= amx::grav_apply(p->grav, old, state, p->ctl, h, *prm, s);
     if (rc) return rc;
+    if (p->cfg.mhd) {
+      rc |= fv_seam(p, state, prm, amx::FV_MODE_MAGNETIC, 1.0, INFINITY, s);
+      rc |= cuda_ok(cudaMemcpyAsync(old, state, gas_bytes, cudaMemcpyDeviceToDevice, s));
+      rc |= fv_seam(p, state, prm, amx::FV_MODE_HYDRO_RK2, h, INFINITY, s);
+      rc |= amx::grav_apply(p->grav, old, state, p->ctl, h, *prm, s);
+    }
   }
+  if (rc) return rc;
   if (!evolve_only) rc = amx::grav_advance(p->ctl, p->dt_hist, p->it_hist, p->max_hist, p->cfg.mhd, s);
   return rc;
 }
@@ -323,6 +339,10 @@ int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out) 
     rc = amx::grav_plan_create(*cfg, &p->grav);
     if (rc) { amx_plan_destroy(p); return rc; }
   }
+  if (cfg->turbulent_forcing) {
+    rc = amx::forcing_plan_create(*cfg, &p->force);
+    if (rc) { amx_plan_destroy(p); return rc; }
+  }
   if (cudaDeviceSynchronize() != cudaSuccess) { amx_plan_destroy(p); return AMX_ERR_CUDA; }
   *out = p;
   return AMX_OK;
@@ -333,6 +353,7 @@ int amx_plan_destroy(amx_plan* p) {
   if (p->diag) cudaFree(p->diag);
   if (p->fd) amx::fd_plan_destroy(p->fd);
   if (p->grav) amx::grav_plan_destroy(p->grav);
+  if (p->force) amx::forcing_plan_destroy(p->force);
   if (p->ws) cudaFree(p->ws);
   delete p;
   return AMX_OK;
@@ -340,7 +361,8 @@ int amx_plan_destroy(amx_plan* p) {
 
 int amx_plan_workspace_bytes(const amx_plan* p, size_t* bytes) {
   if (!p || !bytes) return AMX_ERR_INVALID_ARG;
-  *bytes = p->fd ? amx::fd_workspace_bytes(p->fd) : p->ws_bytes + amx::grav_plan_bytes(p->grav);
+  *bytes = p->fd ? amx::fd_workspace_bytes(p->fd)
+                 : p->ws_bytes + amx::grav_plan_bytes(p->grav) + amx::forcing_plan_bytes(p->force);
   return AMX_OK;
 }
 
@@ -400,13 +422,13 @@ int amx_evolve_state(amx_plan* p, void* state, const amx_params* prm, double dt,
   if (!p || !state || !prm) return AMX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (p->fd) return amx::fd_evolve(p->fd, state, *prm, dt, s);
-  if (p->grav) {
+  if (p->grav) {  // (forcing is not part of _evolve_state_fv)
     const int one = 1;
     int rc = cuda_ok(cudaMemcpyAsync(&p->ctl->dt, &dt, sizeof(double), cudaMemcpyHostToDevice, s));
     rc |= cuda_ok(cudaMemcpyAsync(&p->ctl->active, &one, sizeof(int), cudaMemcpyHostToDevice, s));
     rc |= cuda_ok(cudaStreamSynchronize(s));
     if (rc) return rc;
-    return fv_gravity_step(p, state, prm, INFINITY, true, s);
+    return fv_device_step(p, state, prm, INFINITY, true, s);
   }
   return fv_run_mode(p, state, prm, amx::FV_MODE_EVOLVE, dt, 1.0, 0, false, s);
 }
@@ -437,11 +459,11 @@ int amx_run_async(amx_plan* p, void* state, const amx_params* prm, int64_t max_s
   if (!p || !state || !prm || max_steps < 0) return AMX_ERR_INVALID_ARG;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (p->fd) return amx::fd_run(p->fd, state, *prm, max_steps, INFINITY, s);
-  if (p->grav) {
+  if (p->grav || p->force) {
     // a step is a sequence of launches: queue max_steps of them (bounded)
     if (max_steps > (1 << 20)) return AMX_ERR_TOO_LARGE;
     for (int64_t i = 0; i < max_steps; ++i) {
-      const int rc = fv_gravity_step(p, state, prm, INFINITY, false, s);
+      const int rc = fv_device_step(p, state, prm, INFINITY, false, s);
       if (rc) return rc;
     }
     return AMX_OK;
@@ -478,14 +500,14 @@ int amx_run_until(amx_plan* p, void* state, const amx_params* prm, int64_t max_s
     amx_run_info tmp;
     return read_info(p, info ? info : &tmp, s);
   }
-  if (p->grav) {
+  if (p->grav || p->force) {
     // device-driven steps, the host checks t after 1, 2, 4, .. 32 steps
     int64_t done = 0, chunk = 1;
     amx_run_info g{};
     while (done < max_steps) {
       const int64_t k = std::min<int64_t>(chunk, max_steps - done);
       for (int64_t i = 0; i < k; ++i) {
-        const int rc = fv_gravity_step(p, state, prm, t_pause, false, s);
+        const int rc = fv_device_step(p, state, prm, t_pause, false, s);
         if (rc) return rc;
       }
       done += k;

@@ -79,7 +79,8 @@ int max_resident(const BatchKernelInfo& k, int* per_sm) {
 int validate_template(const amx_config* c) {
   if (!c) return AMX_ERR_INVALID_ARG;
   if (c->solver_mode != AMX_FINITE_VOLUME) return AMX_ERR_UNSUPPORTED;
-  if (c->self_gravity) return AMX_ERR_UNSUPPORTED;  // needs the Poisson solve between phases
+  // need cuFFT work between the phases of a step
+  if (c->self_gravity || c->turbulent_forcing || c->stellar_wind) return AMX_ERR_UNSUPPORTED;
   if (c->dtype != AMX_F32 && c->dtype != AMX_F64) return AMX_ERR_INVALID_ARG;
   if (c->dimensionality != 2) return AMX_ERR_UNSUPPORTED;
   if (c->num_vars != 4 + (c->mhd ? 3 : 0)) return AMX_ERR_INVALID_ARG;

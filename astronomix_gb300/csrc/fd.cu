@@ -12,6 +12,7 @@
 
 #include "fd_api.h"
 #include "fd_kernels.cuh"
+#include "forcing.h"
 
 namespace amx {
 namespace fd {
@@ -31,6 +32,8 @@ struct FDPlan {
   size_t ws_bytes = 0;
   unsigned char* ws = nullptr;
   fd::FDLaunch L{};
+  double wind_V = 0.0;              // stellar wind: sum of the injection mask x dx^3
+  ForcingPlan* force = nullptr;     // turbulent forcing (null without)
 };
 
 namespace {
@@ -57,7 +60,38 @@ fd::FDArgs make_args(const FDPlan* p, const amx_params& prm, double t_pause) {
   a.fixed_timestep = p->cfg.fixed_timestep;
   a.dt_fixed = p->cfg.num_timesteps > 0 ? prm.t_end / p->cfg.num_timesteps : 0.0;
   a.t_pause = t_pause;
+  a.wind = p->cfg.stellar_wind;
+  a.wind_mdot = prm.wind_mass_loss_rate;
+  a.wind_vinf = prm.wind_final_velocity;
+  a.wind_V = p->wind_V;
+  a.wind_rinj = p->cfg.num_injection_cells * p->cfg.grid_spacing;
+  a.wind_r1 = 1.3 * a.wind_rinj;
+  a.box = p->cfg.box_size;
   return a;
+}
+
+// V = sum over cells of the wind's injection mask x dx^3 (stellar_wind.py:503-522),
+// summed over the cube that holds the taper
+double wind_volume(const amx_config& c) {
+  const int n = c.num_cells;
+  const double dx = c.grid_spacing, half = c.box_size / 2;
+  const double rinj = c.num_injection_cells * dx, r1 = 1.3 * rinj;
+  double sum = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double x = dx / 2 + i * dx - half;
+    if (std::fabs(x) > r1) continue;
+    for (int j = 0; j < n; ++j) {
+      const double y = dx / 2 + j * dx - half;
+      if (std::fabs(y) > r1) continue;
+      for (int k = 0; k < n; ++k) {
+        const double z = dx / 2 + k * dx - half;
+        const double r = std::sqrt(x * x + y * y + z * z);
+        if (r <= rinj) sum += 1.0;
+        else if (r <= r1) sum += (r1 - r) / (r1 - rinj);
+      }
+    }
+  }
+  return sum * std::pow(dx, 3);
 }
 
 int stages(FDPlan* p, void* state, const fd::FDArgs& a, cudaStream_t s) {
@@ -98,17 +132,23 @@ int fd_plan_create(const amx_config& cfg, int64_t max_history, FDPlan** out) {
   p->L.grid = (int)(want < (long long)sms * 8 ? want : (long long)sms * 8);
   int rc = (cfg.dtype == AMX_F32) ? fd::fd_set_attrs_f32() : fd::fd_set_attrs_f64();
   if (rc || cudaDeviceSynchronize() != cudaSuccess) { cudaFree(p->ws); delete p; return AMX_ERR_CUDA; }
+  if (cfg.stellar_wind) p->wind_V = wind_volume(cfg);
+  if (cfg.turbulent_forcing) {
+    rc = forcing_plan_create(cfg, &p->force);
+    if (rc) { fd_plan_destroy(p); return rc; }
+  }
   *out = p;
   return AMX_OK;
 }
 
 void fd_plan_destroy(FDPlan* p) {
   if (!p) return;
+  if (p->force) forcing_plan_destroy(p->force);
   if (p->ws) cudaFree(p->ws);
   delete p;
 }
 
-size_t fd_workspace_bytes(const FDPlan* p) { return p->ws_bytes; }
+size_t fd_workspace_bytes(const FDPlan* p) { return p->ws_bytes + forcing_plan_bytes(p->force); }
 
 int fd_reset(FDPlan* p, cudaStream_t s) { return ok(cudaMemsetAsync(p->L.ctl, 0, sizeof(fd::FDControl), s)); }
 
@@ -149,6 +189,8 @@ int fd_run(FDPlan* p, void* state, const amx_params& prm, int64_t max_steps, dou
   const int64_t check_every = 4;
   for (int64_t st = 0; st < max_steps; ++st) {
     int rc = cfl(p, state, a, s);
+    // turbulent forcing between the dt and the evolve (time_integration.py:700-711)
+    if (p->force) rc |= forcing_apply(p->force, state, &p->L.ctl->dt, &p->L.ctl->active, &p->L.ctl->steps, prm, s);
     rc |= stages(p, state, a, s);
     if (rc) return rc;
     if ((st + 1) % check_every == 0 && st + 1 < max_steps) {

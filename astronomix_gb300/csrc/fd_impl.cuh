@@ -407,6 +407,33 @@ __global__ void __launch_bounds__(kThreads) k_emf_avg(Bufs<T> b) {
   }
 }
 
+// The stellar-wind EI source of one cell over the stage's k2 dt
+// (stellar_wind.py:485-584), added to the stage's right-hand side
+// (_ssprk.py:230-241): the tapered mask (1 inside r_inj, linear to 0 at
+// 1.3 r_inj), mass drho/dt = Mdot / V, thermal energy 1/2 v_inf^2 Mdot / V,
+// and the momentum rescaled by sqrt(1 + drho / rho) - 1 so the kinetic
+// energy stays.  q: the stage's cell-centre-refreshed conserved state.
+// Returns false (no source) outside the taper.
+template <typename T>
+__device__ __forceinline__ bool wind_source(const FDArgs& a, int i, int j, int k, const T* qc, long long nc,
+                                            long long c, T dtw, T* src) {
+  const double dx = a.dx, half = a.box / 2;
+  // helper_data.r: cell centres dx/2 + i dx, distance from the box centre
+  const double x = dx / 2 + i * dx - half, y = dx / 2 + j * dx - half, z = dx / 2 + k * dx - half;
+  const double r = sqrt(x * x + y * y + z * z);
+  if (!(r <= a.wind_r1)) return false;
+  const double mask = (r <= a.wind_rinj) ? 1.0 : (a.wind_r1 - r) / (a.wind_r1 - a.wind_rinj);
+  const double drho_dt = a.wind_mdot / a.wind_V;
+  const double dtd = (double)dtw;
+  src[0] = T(drho_dt * mask * dtd);
+  const double dE = 0.5 * (a.wind_vinf * a.wind_vinf) * a.wind_mdot / a.wind_V * dtd;
+  const double f = sqrt(1.0 + drho_dt * dtd * mask / (double)qc[c]) - 1.0;
+#pragma unroll
+  for (int r_ = 1; r_ <= 3; ++r_) src[r_] = T((double)qc[r_ * nc + c] * f);
+  src[4] = T(dE * mask);
+  return true;
+}
+
 // RHS and the SSPRK(5,4) combination (_ssprk.py:224-228, :298-310, :328-332)
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
@@ -435,10 +462,16 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
     rb[0] = -dtdx * D6(Oz, 1) + dtdx * D6(Oy, 2);
     rb[1] = -dtdx * D6(Ox, 2) + dtdx * D6(Oz, 0);
     rb[2] = -dtdx * D6(Oy, 0) + dtdx * D6(Ox, 1);
+    T ws[5] = {T(0), T(0), T(0), T(0), T(0)};
+    const bool wind = a.wind && wind_source<T>(a, i, j, k, b.QC, nc, c, k2 * dt, ws);
+    auto rhs = [&](int r) {
+      const T rq = -dtdx * b.ACC[r * nc + c];
+      return (wind && r < 5) ? rq + ws[r] : rq;
+    };
     if (stage < 4) {
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
-        const T rq = -dtdx * b.ACC[r * nc + c];
+        const T rq = rhs(r);
         const T q = k0 * b.Q0[r * nc + c] + kc * b.Q[r * nc + c] + rq;
         b.Q[r * nc + c] = q;
         b.QF[r * nc + c] = b.QF[r * nc + c] + q * f;
@@ -451,7 +484,7 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
       }
     } else {
 #pragma unroll
-      for (int r = 0; r < 8; ++r) b.QF[r * nc + c] = b.QF[r * nc + c] + (-dtdx * b.ACC[r * nc + c]);
+      for (int r = 0; r < 8; ++r) b.QF[r * nc + c] = b.QF[r * nc + c] + rhs(r);
 #pragma unroll
       for (int r = 0; r < 3; ++r) b.BF[r * nc + c] = b.BF[r * nc + c] + rb[r];
     }

@@ -57,6 +57,14 @@ struct FDArgs {
   int fixed_timestep;
   double dt_fixed;
   double t_pause;
+  // stellar wind EI source (stellar_wind.py:485-584); wind = 0: none
+  int wind;
+  double wind_mdot;    // mass-loss rate
+  double wind_vinf;    // final velocity
+  double wind_V;       // sum of the injection mask x dx^3 (computed on the host)
+  double wind_rinj;    // injection radius, num_injection_cells dx
+  double wind_r1;      // 1.3 x the injection radius (end of the taper)
+  double box;          // box size (cell radii from the box centre)
 };
 
 // buffers and launch geometry handed from the host plan to the typed launchers

@@ -1327,8 +1327,13 @@ fv_run_kernel(FVArgs<T> a) {
     return;
   }
   if (a.mode == FV_MODE_EVOLVE) {
+    double dt_in = a.dt_in;
+    if (a.dt_dev) {
+      if (!*(volatile int*)&ctl->active) return;
+      dt_in = *(volatile double*)&ctl->dt;
+    }
     if (!cfl_phase()) return;
-    const T dtT = T(a.dt_in);
+    const T dtT = T(dt_in);
     if (MHD) {
       if (!rk2(dtT / T(2), false)) return;
       const int it = magnetic(dtT);

@@ -64,7 +64,8 @@ int scratch_address(unsigned char** out) {
 int check_config(const amx_config* c) {
   if (!c) return AMX_ERR_INVALID_ARG;
   if (c->solver_mode != AMX_FINITE_VOLUME) return AMX_ERR_UNSUPPORTED;
-  if (c->self_gravity) return AMX_ERR_UNSUPPORTED;  // needs the Poisson solve between phases
+  // need cuFFT work between the phases of a step
+  if (c->self_gravity || c->turbulent_forcing || c->stellar_wind) return AMX_ERR_UNSUPPORTED;
   if (c->dtype != AMX_F32 && c->dtype != AMX_F64) return AMX_ERR_INVALID_ARG;
   if (c->dimensionality < 1 || c->dimensionality > 3 || c->num_cells < 4) return AMX_ERR_INVALID_ARG;
   if (c->num_vars != c->dimensionality + 2 + (c->mhd ? 3 : 0)) return AMX_ERR_INVALID_ARG;

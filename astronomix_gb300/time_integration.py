@@ -48,11 +48,17 @@ def _check_supported(config: SimulationConfig):
         raise NotImplementedError("only Cartesian geometry is part of the accelerated path")
     if config.self_gravity and config.solver_mode != FINITE_VOLUME:
         raise NotImplementedError("self-gravity is part of the finite-volume scheme only")
-    if config.wind_config.stellar_wind or config.cooling_config.cooling or \
-            config.cosmic_ray_config.cosmic_rays or config.neural_net_force_config.neural_net_force or \
-            config.cnn_mhd_corrector_config.cnn_mhd_corrector or \
-            config.turbulent_forcing_config.turbulent_forcing:
+    if config.cooling_config.cooling or config.cosmic_ray_config.cosmic_rays or \
+            config.neural_net_force_config.neural_net_force or config.cnn_mhd_corrector_config.cnn_mhd_corrector:
         raise NotImplementedError("physics modules are not part of the accelerated MHD step")
+    if config.wind_config.stellar_wind and config.solver_mode != FINITE_DIFFERENCE:
+        # the FD scheme's wind is a right-hand-side source (_ssprk.py:230-241); the FV
+        # physics-module injection is not part of the accelerated path
+        raise NotImplementedError("stellar wind is supported as the finite-difference source term")
+    if config.turbulent_forcing_config.turbulent_forcing and (
+            config.dimensionality != 3 or
+            (config.solver_mode == FINITE_VOLUME and config.boundary_handling != PERIODIC_ROLL)):
+        raise ValueError("turbulent forcing acts on the unpadded 3D state (periodic roll)")
     if config.solver_mode == FINITE_VOLUME:
         if config.split == UNSPLIT:
             if config.time_integrator != RK2_SSP:
@@ -112,6 +118,9 @@ def make_amx_config(config: SimulationConfig, rv: RegisteredVariables, shape, dt
     c.use_max_adaptive_timestep = int(bool(config.use_max_adaptive_timestep))
     c.self_gravity = int(bool(config.self_gravity))
     c.self_gravity_version = int(config.self_gravity_version)
+    c.stellar_wind = int(bool(config.wind_config.stellar_wind))
+    c.num_injection_cells = int(config.wind_config.num_injection_cells)
+    c.turbulent_forcing = int(bool(config.turbulent_forcing_config.turbulent_forcing))
     return c
 
 

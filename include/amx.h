@@ -101,6 +101,9 @@ typedef struct amx_config {
   int32_t use_max_adaptive_timestep; /* split: dt = min(dt, dt_max)            */
   int32_t self_gravity;           /* FV: 0 / 1, the source term after every gas update */
   int32_t self_gravity_version;   /* AMX_SIMPLE_SOURCE_TERM .. AMX_HALF_SPLIT  */
+  int32_t stellar_wind;           /* FD (3D): the EI wind source in every stage's right-hand side */
+  int32_t num_injection_cells;    /* wind injection radius in cells            */
+  int32_t turbulent_forcing;      /* 3D: solenoidal forcing before every step  */
   int32_t reserved;
 } amx_config;
 
@@ -113,6 +116,10 @@ typedef struct amx_params {
   double dt_max;
   double t_end;
   double gravitational_constant;  /* self-gravity G                        */
+  double wind_mass_loss_rate;     /* stellar wind (WindParams)             */
+  double wind_final_velocity;
+  double energy_injection_rate;   /* turbulent forcing (TurbulentForcingParams) */
+  int64_t forcing_seed;           /* key of the forcing's random stream    */
 } amx_params;
 
 /* Result of a time-integration call. */

@@ -46,8 +46,15 @@ def evolve(P, dt, config, params, rv, stats=None):
         dt_ = xp.scalar(dt, P)
         return _fv.evolve_state_fv(P, dt_, gamma, config, rv, stats=stats, C_cfl=xp.scalar(params.C_cfl, P),
                                    G=params.gravitational_constant)
+    wind = None
+    if config.wind_config.stellar_wind:
+        from .forcing import cell_radius
+        wp = params.wind_params
+        wind = (wp.wind_mass_loss_rate, wp.wind_final_velocity,
+                cell_radius(config.num_cells, config.grid_spacing, config.box_size),
+                config.wind_config.num_injection_cells)
     return _fd.evolve_state_fd(P, dt, gamma, config.grid_spacing, params.minimum_density,
-                               params.minimum_pressure, config.enforce_positivity)
+                               params.minimum_pressure, config.enforce_positivity, wind)
 
 
 def snapshot_quantities(P_unpadded, config, params, rv):
@@ -118,6 +125,12 @@ def time_integration(state, config, params, rv, time_mode="reference", max_steps
             if config.exact_end_time:
                 dt = min(dt, _dtype_scalar(t_end, P, time_mode) - t) if time_mode == "float64" else \
                     xp.minimum(dt, xp.scalar(t_end, P) - t)
+        if config.turbulent_forcing_config.turbulent_forcing:
+            # time_integration.py:700-711 (Philox noise, see oracle/forcing.py)
+            if ghost:
+                raise ValueError("turbulent forcing needs the unpadded state (periodic roll)")
+            from .forcing import apply_forcing
+            P = apply_forcing(P, dt, steps, config, params, rv)
         P = evolve(P, dt, config, params, rv, stats=its)
         t = t + dt
         dts.append(float(dt))

@@ -492,8 +492,10 @@ K_CURR = (0.0, 0.55562950593266, 0.37989814861460, 0.82192004589227, 5.035809472
 FINAL = (-2.081261929715610e-02, 0.0, 0.51723167208978, -6.518979800418380e-12, 5.03580947213895e-01)
 
 
-def compute_rhs(q, bx, by, bz, k2, dt, dx, gamma, rhomin, pgmin, enforce_pos=True):
-    """_finite_difference/_time_integrators/_ssprk.py:197-243."""
+def compute_rhs(q, bx, by, bz, k2, dt, dx, gamma, rhomin, pgmin, enforce_pos=True, wind=None):
+    """_finite_difference/_time_integrators/_ssprk.py:197-243.  `wind`:
+    (mass-loss rate, final velocity, cell radii, injection cells) for the
+    stellar-wind EI source (:230-241), or None."""
     q = update_cell_center_fields(q, bx, by, bz)
     dtdx = k2 * dt / dx
     Fx = weno_flux(q, 1, rhomin, pgmin, gamma, enforce_pos)
@@ -501,10 +503,14 @@ def compute_rhs(q, bx, by, bz, k2, dt, dx, gamma, rhomin, pgmin, enforce_pos=Tru
     Fz = weno_flux(q, 3, rhomin, pgmin, gamma, enforce_pos)
     rbx, rby, rbz = ct_rhs(q, Fx, Fy, Fz, dtdx, dtdx, dtdx)
     rhs_q = -dtdx * ((Fx - xp.roll(Fx, 1, 1)) + (Fy - xp.roll(Fy, 1, 2)) + (Fz - xp.roll(Fz, 1, 3)))
+    if wind is not None:
+        from .forcing import wind_ei3d_source
+        mdot, vinf, r, nic = wind
+        rhs_q = rhs_q + wind_ei3d_source(q, k2 * dt, mdot, vinf, r, dx, nic)
     return rhs_q, rbx, rby, rbz
 
 
-def ssprk4_with_ct(q0, bx0, by0, bz0, gamma, dx, dt, rhomin, pgmin, enforce_pos=True):
+def ssprk4_with_ct(q0, bx0, by0, bz0, gamma, dx, dt, rhomin, pgmin, enforce_pos=True, wind=None):
     """_ssprk.py:178-347."""
     dt_ = xp.scalar(dt, q0)
     k_rhs = [xp.scalar(k, q0) for k in K_RHS]
@@ -516,7 +522,7 @@ def ssprk4_with_ct(q0, bx0, by0, bz0, gamma, dx, dt, rhomin, pgmin, enforce_pos=
     for s in range(4):
         if enforce_pos:
             q = enforce_positivity(q, gamma, rhomin, pgmin)
-        rq, rbx, rby, rbz = compute_rhs(q, bx, by, bz, k_rhs[s], dt_, dx, gamma, rhomin, pgmin, enforce_pos)
+        rq, rbx, rby, rbz = compute_rhs(q, bx, by, bz, k_rhs[s], dt_, dx, gamma, rhomin, pgmin, enforce_pos, wind)
         q = k_0[s] * q0 + k_c[s] * q + rq
         bx = k_0[s] * bx0 + k_c[s] * bx + rbx
         by = k_0[s] * by0 + k_c[s] * by + rby
@@ -526,7 +532,7 @@ def ssprk4_with_ct(q0, bx0, by0, bz0, gamma, dx, dt, rhomin, pgmin, enforce_pos=
         bxf = bxf + bx * f
         byf = byf + by * f
         bzf = bzf + bz * f
-    rq, rbx, rby, rbz = compute_rhs(q, bx, by, bz, k_rhs[4], dt_, dx, gamma, rhomin, pgmin, enforce_pos)
+    rq, rbx, rby, rbz = compute_rhs(q, bx, by, bz, k_rhs[4], dt_, dx, gamma, rhomin, pgmin, enforce_pos, wind)
     qf = qf + rq
     bxf = bxf + rbx
     byf = byf + rby
@@ -537,11 +543,11 @@ def ssprk4_with_ct(q0, bx0, by0, bz0, gamma, dx, dt, rhomin, pgmin, enforce_pos=
     return qf, bxf, byf, bzf
 
 
-def evolve_state_fd(P, dt, gamma, dx, rhomin, pgmin, enforce_pos=True):
+def evolve_state_fd(P, dt, gamma, dx, rhomin, pgmin, enforce_pos=True, wind=None):
     """_finite_difference/_state_evolution/_evolve_state.py:25-73."""
     U = cons_from_prim(P[:-3], gamma)
     bx, by, bz = P[FACE_X], P[FACE_Y], P[FACE_Z]
-    U, bx, by, bz = ssprk4_with_ct(U, bx, by, bz, gamma, dx, dt, rhomin, pgmin, enforce_pos)
+    U, bx, by, bz = ssprk4_with_ct(U, bx, by, bz, gamma, dx, dt, rhomin, pgmin, enforce_pos, wind)
     Pn = prim_from_cons(U, rhomin, pgmin, gamma, enforce_pos)
     return xp.concatenate([Pn, bx[None], by[None], bz[None]], axis=0)
 

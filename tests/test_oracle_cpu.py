@@ -223,3 +223,55 @@ def test_self_gravity_run_conserves_mass_and_pulls_inward():
     assert abs(out[0].sum() - s[0].sum()) < 1e-12 * s[0].sum()
     # velocity points towards x = 0 mod 1: negative on (0, 1/2), positive on (1/2, 1)
     assert out[1][2:n // 2 - 2].max() < 0 and out[1][n // 2 + 2:-2].min() > 0
+
+
+def test_philox_known_answers():
+    """Philox4x32-10 against the published known-answer vectors (Random123)."""
+    from oracle.forcing import philox4x32_10
+    cases = [((0, 0, 0, 0, 0, 0), (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)),
+             ((0xffffffff,) * 6, (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+             ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344, 0xa4093822, 0x299f31d0),
+              (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1))]
+    for args, want in cases:
+        got = tuple(int(x) for x in philox4x32_10(*args))
+        assert got == want
+
+
+def test_forcing_field_is_solenoidal_and_injects_edot_dt():
+    """_turbulent_forcing.py: the field has no compressive part, and the
+    amplitude injects exactly Edot dt of kinetic energy."""
+    from types import SimpleNamespace
+    from oracle import forcing
+    n, box = 16, 1.0
+    w = forcing.create_forcing_field(42, 3, n, box)
+    k = 2 * np.pi * np.fft.fftfreq(n, d=box / n)
+    kx, ky, kz = np.meshgrid(k, k, k, indexing="ij")
+    wh = [np.fft.fftn(c) for c in w]
+    # the real part symmetrises the spectrum; off the Nyquist planes (where
+    # fftfreq gives -k for both k and -k) that keeps k . w = 0
+    nyq = np.zeros((n, n, n), bool)
+    nyq[n // 2], nyq[:, n // 2], nyq[:, :, n // 2] = True, True, True
+    div = np.abs(np.where(nyq, 0.0, kx * wh[0] + ky * wh[1] + kz * wh[2])).max()
+    assert div < 1e-10 * max(np.abs(h).max() for h in wh) * np.abs(k).max()
+    cfg, prm, rv, s = smooth_random(3, n, seed=1, t_end=0.01)
+    cfg = cfg._replace(num_cells=n, box_size=box, grid_spacing=box / n)
+    prm = prm._replace(turbulent_forcing_params=SimpleNamespace(energy_injection_rate=3.0))
+    dt = 1e-3
+    out = forcing.apply_forcing(s, dt, 3, cfg, prm, rv)
+    ek = lambda P: 0.5 * np.sum(P[0] * (P[1] ** 2 + P[2] ** 2 + P[3] ** 2)) * (box / n) ** 3
+    assert abs((ek(out) - ek(s)) - 3.0 * dt) < 1e-10
+
+
+def test_wind_source_injects_mass_loss_rate():
+    """stellar_wind.py:485-584: one stage's source adds Mdot dt of mass and
+    0.5 v_inf^2 Mdot dt of energy; outside 1.3 r_inj nothing changes."""
+    from oracle import forcing
+    n, box = 24, 1.0
+    dx = box / n
+    r = forcing.cell_radius(n, dx, box)
+    q = np.ones((8, n, n, n))
+    q[1:4] = 0.3
+    src = forcing.wind_ei3d_source(q, 1e-3, 2.0, 3.0, r, dx, 4)
+    assert abs(src[0].sum() * dx ** 3 - 2.0 * 1e-3) < 1e-15
+    assert abs(src[4].sum() * dx ** 3 - 0.5 * 9.0 * 2.0 * 1e-3) < 1e-14
+    assert np.all(src[:, r > 1.3 * 4 * dx] == 0)
