@@ -45,7 +45,7 @@ def run_both(cfg, prm, rv, s):
 
 
 def test_fd_stellar_wind_fp64(cuda):
-    cfg, prm, rv, s = blast_fd(n=16, t_end=0.002)
+    cfg, prm, rv, s = blast_fd(n=16, t_end=0.004)
     cfg, prm = with_wind(cfg, prm)
     got, ref, rec = run_both(cfg, prm, rv, s)
     assert rec["steps"] >= 3
@@ -55,7 +55,7 @@ def test_fd_stellar_wind_fp64(cuda):
 
 
 def test_fd_turbulent_forcing_fp64(cuda):
-    cfg, prm, rv, s = blast_fd(n=16, t_end=0.002)
+    cfg, prm, rv, s = blast_fd(n=16, t_end=0.004)
     cfg, prm = with_forcing(cfg, prm)
     got, ref, rec = run_both(cfg, prm, rv, s)
     assert rec["steps"] >= 3
