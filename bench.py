@@ -262,6 +262,42 @@ def time_arena(solver, n=256, steps=3):
             "steps_timed": steps}
 
 
+def time_fd_sources(n=256, steps=3):
+    """The FD showcase combination on the 256^3 blast (FP32): turbulent
+    forcing (energy injection rate 0.2) before every step and a stellar-wind
+    EI source (8 injection cells) in every stage, against the same run
+    without them."""
+    import torch
+    from astronomix_gb300 import _native
+    from astronomix_gb300.option_classes import (WindConfig, WindParams, TurbulentForcingConfig,
+                                                 TurbulentForcingParams)
+    from astronomix_gb300.time_integration import get_plan
+
+    cfg, prm, rv, s = arena_blast(n, "fd")
+    cfg = cfg._replace(wind_config=WindConfig(stellar_wind=True, num_injection_cells=8),
+                       turbulent_forcing_config=TurbulentForcingConfig(turbulent_forcing=True))
+    prm = prm._replace(wind_params=WindParams(wind_mass_loss_rate=1.0, wind_final_velocity=10.0),
+                       turbulent_forcing_params=TurbulentForcingParams(energy_injection_rate=0.2))
+    plan = get_plan(cfg, rv, s.shape, np.float32)
+    p = _native.make_params(prm)
+    st = torch.cuda.current_stream()
+    dev = torch.from_numpy(s).cuda()
+    plan.reset(st.cuda_stream)
+    plan.run_async(dev.data_ptr(), p, 2, st.cuda_stream)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    plan.run_async(dev.data_ptr(), p, steps, st.cuda_stream)
+    b.record(st)
+    torch.cuda.synchronize()
+    info = plan.run(dev.data_ptr(), p, 0, st.cuda_stream)
+    sps = a.elapsed_time(b) / 1e3 / steps
+    ok = bool(torch.isfinite(dev).all()) and info.status == 0
+    del dev
+    return {"workload": "FD WENO-CT blast %d^3 + turbulent forcing + stellar-wind EI source" % n,
+            "s_per_step": sps, "zone_updates_per_s": n ** 3 / sps, "finite": ok, "steps_timed": steps}
+
+
 def fd_precision(n=128, t_end=0.02, flop_per_zu=44e3):
     """FD WENO-CT on the MHD blast of the FD workload (periodic unit cube,
     rho = 1, p = 10 inside r < 0.1 and 0.1 outside, B = (1, 1, 0)/sqrt 2,
@@ -750,7 +786,9 @@ def run_ours(args, rank, world):
     arena = {}
     if not args.no_arena:
         arena = {"fd_blast_fp32": time_arena("fd"), "fv_lf_blast_fp32": time_arena("fv"),
-                 "fd_blast_fp32_vs_fp64": fd_precision()}
+                 "fd_blast_fp32_vs_fp64": fd_precision(), "fd_blast_forcing_wind_fp32": time_fd_sources()}
+        arena["fd_blast_forcing_wind_fp32"]["overhead_vs_plain"] = (
+            arena["fd_blast_forcing_wind_fp32"]["s_per_step"] / arena["fd_blast_fp32"]["s_per_step"] - 1.0)
     ensemble = None if args.no_ensemble else time_ensemble()
     adjoint = None if args.no_adjoint else time_adjoint()
     gravity = None if args.no_gravity else time_gravity()

@@ -23,6 +23,9 @@ from _cases import blast_fd, smooth_random, rel_err, rel_l1
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-11
+# no field component zero: with B_n = 0 the reference's eigenvectors are
+# ill-conditioned (a 1e-15 perturbation moves its result by 1e-8)
+OBLIQUE = (0.6, 0.5, 0.4)
 
 
 def with_wind(cfg, prm, nic=3, mdot=2.0, vinf=3.0):
@@ -45,7 +48,7 @@ def run_both(cfg, prm, rv, s):
 
 
 def test_fd_stellar_wind_fp64(cuda):
-    cfg, prm, rv, s = blast_fd(n=16, t_end=0.004)
+    cfg, prm, rv, s = blast_fd(n=16, t_end=0.004, B=OBLIQUE)
     cfg, prm = with_wind(cfg, prm)
     got, ref, rec = run_both(cfg, prm, rv, s)
     assert rec["steps"] >= 3
@@ -55,7 +58,7 @@ def test_fd_stellar_wind_fp64(cuda):
 
 
 def test_fd_turbulent_forcing_fp64(cuda):
-    cfg, prm, rv, s = blast_fd(n=16, t_end=0.004)
+    cfg, prm, rv, s = blast_fd(n=16, t_end=0.004, B=OBLIQUE)
     cfg, prm = with_forcing(cfg, prm)
     got, ref, rec = run_both(cfg, prm, rv, s)
     assert rec["steps"] >= 3
@@ -66,7 +69,7 @@ def test_fd_turbulent_forcing_fp64(cuda):
 
 def test_fd_wind_and_forcing_fp64(cuda):
     """The showcase combination: driven turbulence with a wind source."""
-    cfg, prm, rv, s = blast_fd(n=24, t_end=0.0015)
+    cfg, prm, rv, s = blast_fd(n=24, t_end=0.0015, B=OBLIQUE)
     cfg, prm = with_wind(cfg, prm, nic=4)
     cfg, prm = with_forcing(cfg, prm)
     got, ref, _ = run_both(cfg, prm, rv, s)
@@ -74,7 +77,7 @@ def test_fd_wind_and_forcing_fp64(cuda):
 
 
 def test_fd_wind_and_forcing_fp32(cuda):
-    cfg, prm, rv, s = blast_fd(n=24, dtype=np.float32, t_end=0.0015)
+    cfg, prm, rv, s = blast_fd(n=24, dtype=np.float32, t_end=0.0015, B=OBLIQUE)
     cfg, prm = with_wind(cfg, prm, nic=4)
     cfg, prm = with_forcing(cfg, prm)
     got, ref, _ = run_both(cfg, prm, rv, s)
