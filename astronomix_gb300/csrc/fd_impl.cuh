@@ -418,7 +418,13 @@ template <typename T>
 __device__ __forceinline__ bool wind_source(const FDArgs& a, int i, int j, int k, const T* qc, long long nc,
                                             long long c, T dtw, T* src) {
   const double dx = a.dx, half = a.box / 2;
-  // helper_data.r: cell centres dx/2 + i dx, distance from the box centre
+  // helper_data.r: cell centres dx/2 + i dx, distance from the box centre;
+  // cells whose offset along one axis already exceeds the taper are skipped
+  // before any FP64 arithmetic
+  const float lim = (float)(a.wind_r1 / dx) + 1.0f;
+  const float h = 0.5f * (float)a.n;
+  if (fabsf((float)i + 0.5f - h) > lim || fabsf((float)j + 0.5f - h) > lim || fabsf((float)k + 0.5f - h) > lim)
+    return false;
   const double x = dx / 2 + i * dx - half, y = dx / 2 + j * dx - half, z = dx / 2 + k * dx - half;
   const double r = sqrt(x * x + y * y + z * z);
   if (!(r <= a.wind_r1)) return false;

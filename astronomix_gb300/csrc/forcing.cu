@@ -78,43 +78,44 @@ template <> struct FCplx<float> { using type = cufftComplex; };
 template <> struct FCplx<double> { using type = cufftDoubleComplex; };
 
 // The three solenoidal Fourier fields of one step (_turbulent_forcing.py:15-63),
-// in FP64, stored in the state's precision; the inverse transform's 1 / n^3
-// is applied by the readers.
-template <typename C>
+// computed in R (FP64 for FP64 states, FP32 for FP32 ones: GB300's FP64
+// transcendentals would dominate the forcing otherwise); the inverse
+// transform's 1 / n^3 is applied by the readers.
+template <typename C, typename R>
 __global__ void __launch_bounds__(kFThreads) k_force_spectrum(C* W, int n, double box, unsigned long long seed,
                                                               const long long* steps, const int* active) {
   if (!*(volatile const int*)active) return;
   const long long n3 = (long long)n * n * n;
   const unsigned long long step = (unsigned long long)*(volatile const long long*)steps;
-  const double pi = 3.141592653589793;
-  const double val = 1.0 / ((double)n * (box / n));
-  const double kpk = 4.0 * pi / box;
+  const R pi = R(3.141592653589793);
+  const R val = R(1.0 / ((double)n * (box / n)));
+  const R kpk = R(4.0 * 3.141592653589793 / box);
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   for (long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x; m < n3; m += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(m / ((long long)n * n)), j = (int)((m / n) % n), l = (int)(m % n);
-    auto freq = [&](int q) { return (double)((q <= (n - 1) / 2) ? q : q - n) * val; };
-    const double kx = 2.0 * pi * freq(i), ky = 2.0 * pi * freq(j), kz = 2.0 * pi * freq(l);
-    const double k2 = kx * kx + ky * ky + kz * kz;
-    const double kk = sqrt(k2);
-    const double Pk = pow(kk, 6.0) * exp(-8.0 * kk / kpk);
-    const double sq = sqrt(Pk);
-    double re[3], im[3];
+    auto freq = [&](int q) { return R((q <= (n - 1) / 2) ? q : q - n) * val; };
+    const R kx = R(2) * pi * freq(i), ky = R(2) * pi * freq(j), kz = R(2) * pi * freq(l);
+    const R k2 = kx * kx + ky * ky + kz * kz;
+    const R kk = sqrt(k2);
+    const R Pk = pow(kk, R(6)) * exp(R(-8) * kk / kpk);
+    const R sq = sqrt(Pk);
+    R re[3], im[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const Philox4 r = philox4x32_10((uint32_t)m, (uint32_t)c, (uint32_t)step, (uint32_t)(step >> 32), k0, k1);
-      const double u1 = ((double)r.x[0] + 1.0) * 2.3283064365386963e-10;  // 2^-32
-      const double u2 = (double)r.x[1] * 2.3283064365386963e-10;
-      const double rr = sqrt(-2.0 * log(u1));
-      const double th = 2.0 * pi * u2;
-      re[c] = m == 0 ? 0.0 : sq * (rr * cos(th));
-      im[c] = m == 0 ? 0.0 : sq * (rr * sin(th));
+      const R u1 = R(((double)r.x[0] + 1.0) * 2.3283064365386963e-10);  // 2^-32
+      const R u2 = R((double)r.x[1] * 2.3283064365386963e-10);
+      const R rr = sqrt(R(-2) * log(u1));
+      const R th = R(2) * pi * u2;
+      re[c] = m == 0 ? R(0) : sq * (rr * cos(th));
+      im[c] = m == 0 ? R(0) : sq * (rr * sin(th));
     }
     // project out the compressive part: w -= k (k . w) / k^2
-    const double k2s = (k2 == 0.0) ? 1.0 : k2;
-    double dre = (kx * re[0] + ky * re[1] + kz * re[2]) / k2s;
-    double dim = (kx * im[0] + ky * im[1] + kz * im[2]) / k2s;
-    if (m == 0) dre = dim = 0.0;
-    const double kv[3] = {kx, ky, kz};
+    const R k2s = (k2 == R(0)) ? R(1) : k2;
+    R dre = (kx * re[0] + ky * re[1] + kz * re[2]) / k2s;
+    R dim = (kx * im[0] + ky * im[1] + kz * im[2]) / k2s;
+    if (m == 0) dre = dim = R(0);
+    const R kv[3] = {kx, ky, kz};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       C z;
@@ -258,7 +259,8 @@ int apply_t(ForcingPlan* f, T* P, const double* dt, const int* active, const lon
   C* W = static_cast<C*>(f->W);
   const long long b = (f->n3 + kFThreads - 1) / kFThreads;
   const int grid = (int)(b < (long long)f->num_sms * 8 ? b : (long long)f->num_sms * 8);
-  k_force_spectrum<C><<<grid, kFThreads, 0, s>>>(W, f->n, f->box, (unsigned long long)prm.forcing_seed, steps, active);
+  k_force_spectrum<C, T><<<grid, kFThreads, 0, s>>>(W, f->n, f->box, (unsigned long long)prm.forcing_seed, steps,
+                                                     active);
   if (cudaGetLastError() != cudaSuccess) return AMX_ERR_CUDA;
   if (cufftSetStream(f->plan, s) != CUFFT_SUCCESS) return AMX_ERR_CUDA;
   cufftResult r;
