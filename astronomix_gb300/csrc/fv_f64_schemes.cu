@@ -8,7 +8,7 @@ namespace amx {
 #define AMX_FV_SCHEME_CASE(D, R, M, S)                                       \
   if (dim == D && rs == R && mhd == M && scheme == S) {                      \
     out->fn = (const void*)&fv_run_kernel<double, D, R, M, S>;                 \
-    out->smem = TileGeom<double, D>::SMEM;                                     \
+    out->smem = S == FV_SPLIT ? TileGeom<double, D>::SPLIT_SMEM : TileGeom<double, D>::SMEM; \
     out->smem_pp = TileGeom<double, D>::PP_SMEM;                               \
     return true;                                                             \
   }

@@ -176,6 +176,14 @@ struct TileGeom {
   static constexpr int B0 = T0 + 2, B1 = (DIM >= 2) ? T1 + 2 : 1, B2 = (DIM >= 3) ? T2 + 2 : 1;
   static constexpr int BOX = B0 * B1 * B2;
   static constexpr size_t PP_SMEM = sizeof(T) * (size_t)DIM * NV * BOX;
+  // split sweep along axis k: the tile with a halo of 2 along k, the faces
+  // along k, and the interface states (left / right) of the cells beside them
+  static constexpr int X0 = (T0 + 4) * T1 * T2 + (T0 + 1) * T1 * T2 + 2 * (T0 + 2) * T1 * T2;
+  static constexpr int X1 = (DIM >= 2) ? T0 * ((T1 + 4) + (T1 + 1) + 2 * (T1 + 2)) * T2 : 0;
+  static constexpr int X2 = (DIM >= 3) ? T0 * T1 * ((T2 + 4) + (T2 + 1) + 2 * (T2 + 2)) : 0;
+  static constexpr int XMAX = X0 > X1 ? (X0 > X2 ? X0 : X2) : (X1 > X2 ? X1 : X2);
+  static constexpr size_t SPLIT_SMEM0 = sizeof(T) * (size_t)NV * XMAX;
+  static constexpr size_t SPLIT_SMEM = SPLIT_SMEM0 > SMEM ? SPLIT_SMEM0 : SMEM;
 };
 
 template <int DIM>
@@ -595,7 +603,9 @@ __device__ __forceinline__ void muscl_states(const T* qm, const T* q0, const T* 
 // One split sweep of a tile along axis k (evolve_state.py:52-160):
 // interface states (MUSCL-Hancock, or piecewise constant with
 // first_order), Riemann fluxes along k, U += (1/dx)(F[i-1/2] - F[i+1/2]) dt.
-// The tile carries a halo of 2 along k only.
+// The tile carries a halo of 2 along k only.  The MUSCL-Hancock states of
+// every cell beside a face are computed once into shared memory (both faces
+// of a cell read them) before the Riemann pass.
 template <typename T, int DIM, int RS>
 __device__ __forceinline__ void sweep_tile(const FVArgs<T>& a, const int* o, int k, const T* __restrict__ Pin,
                                            T* Pout, T dt, const T* alpha, T* smem, T* m, bool track) {
@@ -616,8 +626,15 @@ __device__ __forceinline__ void sweep_tile(const FVArgs<T>& a, const int* o, int
   const int F0 = G::T0 + (k == 0), F1 = (DIM >= 2) ? G::T1 + (k == 1) : 1, F2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
   const int NF = F0 * F1 * F2;
   const int stride = (k == 0) ? E1 * E2 : ((k == 1) ? E2 : 1);
+  // the cells beside a face along k: halo index 1 .. E_k - 2 along k
+  const int S0 = G::T0 + 2 * (k == 0), S1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1,
+            S2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
+  const int NS = S0 * S1 * S2;
+  const int sstride = (k == 0) ? S1 * S2 : ((k == 1) ? S2 : 1);
   T* sP = smem;            // [NV][HL]
   T* sF = smem + NV * HL;  // [NV][NF]
+  T* sLo = sF + NV * NF;   // [NV][NS] left-face state of each cell
+  T* sHi = sLo + NV * NS;  // [NV][NS] right-face state
   for (int e = threadIdx.x; e < HL; e += blockDim.x) {
     const int e2 = e % E2, e1 = (e / E2) % E1, e0 = e / (E2 * E1);
     bool f0 = false, f1 = false, f2 = false;
@@ -633,31 +650,45 @@ __device__ __forceinline__ void sweep_tile(const FVArgs<T>& a, const int* o, int
     }
   }
   __syncthreads();
+  if (!first_order) {
+    // MUSCL-Hancock states of the cells beside the faces, once per cell
+    for (int e = threadIdx.x; e < NS; e += blockDim.x) {
+      const int s2 = e % S2, s1 = (e / S2) % S1, s0 = e / (S2 * S1);
+      const int h = ((s0 + (k == 0)) * E1 + (DIM >= 2 ? s1 + (k == 1) : 0)) * E2 + (DIM >= 3 ? s2 + (k == 2) : 0);
+      T qm[NV], q0[NV], qp[NV], lo[NV], hi[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        qm[v] = sP[v * HL + h - stride];
+        q0[v] = sP[v * HL + h];
+        qp[v] = sP[v * HL + h + stride];
+      }
+      muscl_states<T, DIM>(qm, q0, qp, k + 1, gamma, dt, dxT, limiter, lo, hi);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        sLo[v * NS + e] = lo[v];
+        sHi[v * NS + e] = hi[v];
+      }
+    }
+    __syncthreads();
+  }
   for (int f = threadIdx.x; f < NF; f += blockDim.x) {
     const int f2 = f % F2, f1 = (f / F2) % F1, f0 = f / (F2 * F1);
-    // halo index of the cell right of the face
-    const int hr = ((f0 + 2 * (k == 0)) * E1 + (DIM >= 2 ? f1 + 2 * (k == 1) : 0)) * E2 +
-                   (DIM >= 3 ? f2 + 2 * (k == 2) : 0);
-    const int hl = hr - stride;
     T qL[NV], qR[NV];
     if (first_order) {
+      // halo index of the cell right of the face
+      const int hr = ((f0 + 2 * (k == 0)) * E1 + (DIM >= 2 ? f1 + 2 * (k == 1) : 0)) * E2 +
+                     (DIM >= 3 ? f2 + 2 * (k == 2) : 0);
+      const int hl = hr - stride;
 #pragma unroll
       for (int v = 0; v < NV; ++v) { qL[v] = sP[v * HL + hl]; qR[v] = sP[v * HL + hr]; }
     } else {
-      T lm1[NV], l0[NV], lp1[NV], rp1[NV], lo[NV], hi[NV];
+      // the left cell of the face has index f_k along k in the state box, the right one f_k + 1
+      const int sl = (f0 * S1 + (DIM >= 2 ? f1 : 0)) * S2 + (DIM >= 3 ? f2 : 0);
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        lm1[v] = sP[v * HL + hl - stride];
-        l0[v] = sP[v * HL + hl];
-        lp1[v] = sP[v * HL + hr];
-        rp1[v] = sP[v * HL + hr + stride];
+        qL[v] = sHi[v * NS + sl];            // right extrapolation of the left cell
+        qR[v] = sLo[v * NS + sl + sstride];  // left extrapolation of the right cell
       }
-      muscl_states<T, DIM>(lm1, l0, lp1, k + 1, gamma, dt, dxT, limiter, lo, hi);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) qL[v] = hi[v];  // right extrapolation of the left cell
-      muscl_states<T, DIM>(l0, lp1, rp1, k + 1, gamma, dt, dxT, limiter, lo, hi);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) qR[v] = lo[v];  // left extrapolation of the right cell
     }
     T F[NV];
     riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), lm, F);
