@@ -279,6 +279,14 @@ struct GravPlan {
   int num_sms = 1;
   cufftHandle fwd = 0, inv = 0;
   bool have_fwd = false, have_inv = false;
+  // open boundaries in 2D / 3D: the transforms skip the zero half of the
+  // padded grid along x (the density lives in planes x < M, the potential is
+  // read there): a (d-1)-dimensional R2C / C2R over the planes x < M and a
+  // strided 1D C2C along x over the whole half spectrum
+  bool pruned = false;
+  cufftHandle outer = 0;
+  bool have_outer = false;
+  void* spec2 = nullptr;  // pruned: the x-transformed half spectrum (spec keeps its planes x >= M zero)
   unsigned char* mem = nullptr;
   size_t bytes = 0;
   void* fin = nullptr;    // FFT input (E^d real)
@@ -311,10 +319,14 @@ int solver_create(const GravGrid& g, double dx, bool periodic, int dtype, int ol
   const size_t elem = dtype == AMX_F32 ? 4 : 8;
   const long long nreal = ipow_ll(g.E, g.dim);
   const long long ncplx = ipow_ll(g.E, g.dim - 1) * (g.E / 2 + 1);
+  p->pruned = !periodic && g.dim >= 2;
+  // pruned: the real arrays hold the planes x < M only
+  const long long nreal_buf = p->pruned ? (long long)g.M * ipow_ll(g.E, g.dim - 1) : nreal;
   size_t off = 0;
-  const size_t o_in = off; off = align256(off + elem * nreal);
-  const size_t o_out = off; off = align256(off + elem * nreal);
+  const size_t o_in = off; off = align256(off + elem * nreal_buf);
+  const size_t o_out = off; off = align256(off + elem * nreal_buf);
   const size_t o_sp = off; off = align256(off + 2 * elem * ncplx);
+  const size_t o_sp2 = off; off = align256(off + (p->pruned ? 2 * elem * ncplx : 0));
   const size_t o_ks = off; off = align256(off + (periodic ? 1 : 2) * elem * ncplx);
   const size_t o_old = off; off = align256(off + elem * (size_t)old_rows * ncells);
   const size_t o_eacc = off; off = align256(off + (old_rows ? elem * (size_t)ncells : 0));
@@ -327,6 +339,7 @@ int solver_create(const GravGrid& g, double dx, bool periodic, int dtype, int ol
   p->fin = p->mem + o_in;
   p->fout = p->mem + o_out;
   p->spec = p->mem + o_sp;
+  p->spec2 = p->pruned ? p->mem + o_sp2 : nullptr;
   p->kspec = p->mem + o_ks;
   p->old = old_rows ? p->mem + o_old : nullptr;
   p->eacc = old_rows ? p->mem + o_eacc : nullptr;
@@ -334,13 +347,33 @@ int solver_create(const GravGrid& g, double dx, bool periodic, int dtype, int ol
   p->counter = reinterpret_cast<unsigned int*>(p->mem + o_cnt);
   p->mean = reinterpret_cast<double*>(p->mem + o_mean);
   int nn[3] = {g.E, g.E, g.E};
-  int rc = fft_ok(cufftPlanMany(&p->fwd, g.dim, nn, nullptr, 1, 0, nullptr, 1, 0,
-                                dtype == AMX_F32 ? CUFFT_R2C : CUFFT_D2Z, 1));
-  p->have_fwd = rc == AMX_OK;
-  if (!rc) {
-    rc = fft_ok(cufftPlanMany(&p->inv, g.dim, nn, nullptr, 1, 0, nullptr, 1, 0,
-                              dtype == AMX_F32 ? CUFFT_C2R : CUFFT_Z2D, 1));
-    p->have_inv = rc == AMX_OK;
+  int rc;
+  if (!p->pruned) {
+    rc = fft_ok(cufftPlanMany(&p->fwd, g.dim, nn, nullptr, 1, 0, nullptr, 1, 0,
+                              dtype == AMX_F32 ? CUFFT_R2C : CUFFT_D2Z, 1));
+    p->have_fwd = rc == AMX_OK;
+    if (!rc) {
+      rc = fft_ok(cufftPlanMany(&p->inv, g.dim, nn, nullptr, 1, 0, nullptr, 1, 0,
+                                dtype == AMX_F32 ? CUFFT_C2R : CUFFT_Z2D, 1));
+      p->have_inv = rc == AMX_OK;
+    }
+  } else {
+    // (d-1)-dimensional transforms of the M planes x < M (contiguous planes)
+    rc = fft_ok(cufftPlanMany(&p->fwd, g.dim - 1, nn, nullptr, 1, 0, nullptr, 1, 0,
+                              dtype == AMX_F32 ? CUFFT_R2C : CUFFT_D2Z, g.M));
+    p->have_fwd = rc == AMX_OK;
+    if (!rc) {
+      rc = fft_ok(cufftPlanMany(&p->inv, g.dim - 1, nn, nullptr, 1, 0, nullptr, 1, 0,
+                                dtype == AMX_F32 ? CUFFT_C2R : CUFFT_Z2D, g.M));
+      p->have_inv = rc == AMX_OK;
+    }
+    if (!rc) {
+      // 1D along x, one transform per (y, kz) of the half spectrum
+      const int S = (int)(ncplx / g.E);
+      int ne[1] = {g.E};
+      rc = fft_ok(cufftPlanMany(&p->outer, 1, ne, ne, S, 1, ne, S, 1, dtype == AMX_F32 ? CUFFT_C2C : CUFFT_Z2Z, S));
+      p->have_outer = rc == AMX_OK;
+    }
   }
   const double inv_total = 1.0 / (double)nreal;
   if (!rc && periodic) {
@@ -395,7 +428,6 @@ int potential(GravPlan* p, const T* rho, double G, const int* active, cudaStream
   using C = typename Cplx<T>::type;
   const GravGrid& g = p->g;
   const long long nsolve = ipow_ll(g.M, g.dim);
-  const long long nreal = ipow_ll(g.E, g.dim);
   const long long ncplx = ipow_ll(g.E, g.dim - 1) * (g.E / 2 + 1);
   const int grid = grid_for(nsolve, p->num_sms);
   if (p->periodic) {
@@ -407,6 +439,7 @@ int potential(GravPlan* p, const T* rho, double G, const int* active, cudaStream
   int rc = cuda_ok(cudaGetLastError());
   rc |= fft_ok(cufftSetStream(p->fwd, s));
   rc |= fft_ok(cufftSetStream(p->inv, s));
+  if (p->pruned) rc |= fft_ok(cufftSetStream(p->outer, s));
   if (rc) return rc;
   if (sizeof(T) == 4) {
     rc = fft_ok(cufftExecR2C(p->fwd, static_cast<cufftReal*>(p->fin), static_cast<cufftComplex*>(p->spec)));
@@ -414,19 +447,37 @@ int potential(GravPlan* p, const T* rho, double G, const int* active, cudaStream
     rc = fft_ok(cufftExecD2Z(p->fwd, static_cast<cufftDoubleReal*>(p->fin), static_cast<cufftDoubleComplex*>(p->spec)));
   }
   if (rc) return rc;
+  // pruned: along x out of place, so that spec keeps its zero planes x >= M
+  C* sp = static_cast<C*>(p->pruned ? p->spec2 : p->spec);
+  if (p->pruned) {
+    if (sizeof(T) == 4)
+      rc = fft_ok(cufftExecC2C(p->outer, static_cast<cufftComplex*>(p->spec), reinterpret_cast<cufftComplex*>(sp),
+                               CUFFT_FORWARD));
+    else
+      rc = fft_ok(cufftExecZ2Z(p->outer, static_cast<cufftDoubleComplex*>(p->spec),
+                               reinterpret_cast<cufftDoubleComplex*>(sp), CUFFT_FORWARD));
+    if (rc) return rc;
+  }
   const int cgrid = grid_for(ncplx, p->num_sms);
   if (p->periodic)
-    k_spec_scale<C, T><<<cgrid, kGThreads, 0, s>>>(static_cast<C*>(p->spec), static_cast<const T*>(p->kspec), ncplx,
-                                                   T(G), active);
+    k_spec_scale<C, T><<<cgrid, kGThreads, 0, s>>>(sp, static_cast<const T*>(p->kspec), ncplx, T(G), active);
   else
-    k_spec_mul<C, T><<<cgrid, kGThreads, 0, s>>>(static_cast<C*>(p->spec), static_cast<const C*>(p->kspec), ncplx,
-                                                 T(G), active);
+    k_spec_mul<C, T><<<cgrid, kGThreads, 0, s>>>(sp, static_cast<const C*>(p->kspec), ncplx, T(G), active);
   rc = cuda_ok(cudaGetLastError());
   if (rc) return rc;
+  if (p->pruned) {
+    if (sizeof(T) == 4)
+      rc = fft_ok(cufftExecC2C(p->outer, reinterpret_cast<cufftComplex*>(sp), reinterpret_cast<cufftComplex*>(sp),
+                               CUFFT_INVERSE));
+    else
+      rc = fft_ok(cufftExecZ2Z(p->outer, reinterpret_cast<cufftDoubleComplex*>(sp),
+                               reinterpret_cast<cufftDoubleComplex*>(sp), CUFFT_INVERSE));
+    if (rc) return rc;
+  }
   if (sizeof(T) == 4) {
-    rc = fft_ok(cufftExecC2R(p->inv, static_cast<cufftComplex*>(p->spec), static_cast<cufftReal*>(p->fout)));
+    rc = fft_ok(cufftExecC2R(p->inv, reinterpret_cast<cufftComplex*>(sp), static_cast<cufftReal*>(p->fout)));
   } else {
-    rc = fft_ok(cufftExecZ2D(p->inv, static_cast<cufftDoubleComplex*>(p->spec), static_cast<cufftDoubleReal*>(p->fout)));
+    rc = fft_ok(cufftExecZ2D(p->inv, reinterpret_cast<cufftDoubleComplex*>(sp), static_cast<cufftDoubleReal*>(p->fout)));
   }
   return rc;
 }
@@ -490,6 +541,7 @@ void grav_plan_destroy(GravPlan* p) {
   if (!p) return;
   if (p->have_fwd) cufftDestroy(p->fwd);
   if (p->have_inv) cufftDestroy(p->inv);
+  if (p->have_outer) cufftDestroy(p->outer);
   if (p->mem) cudaFree(p->mem);
   delete p;
 }
