@@ -606,10 +606,13 @@ __device__ __forceinline__ void muscl_states(const T* qm, const T* q0, const T* 
 // The tile carries a halo of 2 along k only.  The MUSCL-Hancock states of
 // every cell beside a face are computed once into shared memory (both faces
 // of a cell read them) before the Riemann pass.
-template <typename T, int DIM, int RS>
-__device__ __forceinline__ void sweep_tile(const FVArgs<T>& a, const int* o, int k, const T* __restrict__ Pin,
-                                           T* Pout, T dt, const T* alpha, T* smem, T* m, bool track) {
+template <typename T, int DIM, int RS, int K>
+__device__ __forceinline__ void sweep_tile(const FVArgs<T>& a, const int* o, const T* __restrict__ Pin, T* Pout,
+                                           T dt, const T* alpha, T* smem, T* m, bool track) {
   using G = TileGeom<T, DIM>;
+  // the axis is a compile-time constant: the tile extents below are then
+  // constants and the index arithmetic of every loop avoids integer division
+  constexpr int k = K;
   constexpr int NV = G::NV;
   const int n = a.n;
   const long long nc = a.ncells;
@@ -620,17 +623,18 @@ __device__ __forceinline__ void sweep_tile(const FVArgs<T>& a, const int* o, int
   const bool lm = a.lm != 0;
   const bool first_order = a.first_order != 0;
   const AxisMap<DIM> amap(a);
-  const int E0 = G::T0 + 4 * (k == 0), E1 = (DIM >= 2) ? G::T1 + 4 * (k == 1) : 1,
-            E2 = (DIM >= 3) ? G::T2 + 4 * (k == 2) : 1;
-  const int HL = E0 * E1 * E2;
-  const int F0 = G::T0 + (k == 0), F1 = (DIM >= 2) ? G::T1 + (k == 1) : 1, F2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
-  const int NF = F0 * F1 * F2;
-  const int stride = (k == 0) ? E1 * E2 : ((k == 1) ? E2 : 1);
+  constexpr int E0 = G::T0 + 4 * (k == 0), E1 = (DIM >= 2) ? G::T1 + 4 * (k == 1) : 1,
+                E2 = (DIM >= 3) ? G::T2 + 4 * (k == 2) : 1;
+  constexpr int HL = E0 * E1 * E2;
+  constexpr int F0 = G::T0 + (k == 0), F1 = (DIM >= 2) ? G::T1 + (k == 1) : 1,
+                F2 = (DIM >= 3) ? G::T2 + (k == 2) : 1;
+  constexpr int NF = F0 * F1 * F2;
+  constexpr int stride = (k == 0) ? E1 * E2 : ((k == 1) ? E2 : 1);
   // the cells beside a face along k: halo index 1 .. E_k - 2 along k
-  const int S0 = G::T0 + 2 * (k == 0), S1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1,
-            S2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
-  const int NS = S0 * S1 * S2;
-  const int sstride = (k == 0) ? S1 * S2 : ((k == 1) ? S2 : 1);
+  constexpr int S0 = G::T0 + 2 * (k == 0), S1 = (DIM >= 2) ? G::T1 + 2 * (k == 1) : 1,
+                S2 = (DIM >= 3) ? G::T2 + 2 * (k == 2) : 1;
+  constexpr int NS = S0 * S1 * S2;
+  constexpr int sstride = (k == 0) ? S1 * S2 : ((k == 1) ? S2 : 1);
   T* sP = smem;            // [NV][HL]
   T* sF = smem + NV * HL;  // [NV][NF]
   T* sLo = sF + NV * NF;   // [NV][NS] left-face state of each cell
@@ -696,7 +700,7 @@ __device__ __forceinline__ void sweep_tile(const FVArgs<T>& a, const int* o, int
     for (int v = 0; v < NV; ++v) sF[v * NF + f] = F[v];
   }
   __syncthreads();
-  const int fstride = (k == 0) ? F1 * F2 : ((k == 1) ? F2 : 1);
+  constexpr int fstride = (k == 0) ? F1 * F2 : ((k == 1) ? F2 : 1);
   for (int cl = threadIdx.x; cl < G::CELLS; cl += blockDim.x) {
     const int c2 = cl % G::T2, c1 = (cl / G::T2) % G::T1, c0 = cl / (G::T2 * G::T1);
     const int g0 = o[0] + c0, g1 = o[1] + c1, g2 = o[2] + c2;
@@ -729,7 +733,12 @@ __device__ __noinline__ void phase_sweep(const FVArgs<T>& a, int k, const T* __r
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int o[3];
     tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
-    sweep_tile<T, DIM, RS>(a, o, k, Pin, Pout, dt, alpha, smem, m, out_slot != nullptr);
+    if (k == 0)
+      sweep_tile<T, DIM, RS, 0>(a, o, Pin, Pout, dt, alpha, smem, m, out_slot != nullptr);
+    else if (DIM >= 2 && k == 1)
+      sweep_tile<T, DIM, RS, (DIM >= 2 ? 1 : 0)>(a, o, Pin, Pout, dt, alpha, smem, m, out_slot != nullptr);
+    else if (DIM >= 3)
+      sweep_tile<T, DIM, RS, (DIM >= 3 ? 2 : 0)>(a, o, Pin, Pout, dt, alpha, smem, m, out_slot != nullptr);
   }
   if (out_slot) fold_maxima<DIM>(m, out_slot, red);
 }
