@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-run batched ensemble")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 128^3 adjoint workload")
     ap.add_argument("--no-gravity", action="store_true", help="skip the self-gravity collapse workload")
-    ap.add_argument("--case", default=None, choices=["fd", "fv3d", "ensemble", "adjoint", "gravity"],
+    ap.add_argument("--case", default=None, choices=["fd", "fdsrc", "fv3d", "ensemble", "adjoint", "gravity"],
                     help="run one small case of a secondary workload and exit (for profilers)")
     return ap.parse_args()
 
@@ -64,7 +64,8 @@ def run_case(name):
     density-perturbation problem at 96^3 to t = 0.01, forward and backward
     with the stored tape (a 4 GB tape budget: the case holds a few GB at
     most); gravity: Evrard's collapse at 128^3 FP32, 3 steps of the
-    self-gravity step sequence."""
+    self-gravity step sequence; fdsrc: the FD blast at 128^3 FP32 with
+    turbulent forcing and the stellar-wind source, 2 steps."""
     import torch
     from astronomix_gb300 import _native
 
@@ -72,6 +73,22 @@ def run_case(name):
         from astronomix_gb300.time_integration import get_plan
 
         cfg, prm, rv, s = arena_blast(128 if name == "fd" else 192, name[:2])
+        plan = get_plan(cfg, rv, s.shape, np.float32)
+        dev = torch.from_numpy(s).cuda()
+        st = torch.cuda.current_stream().cuda_stream
+        plan.reset(st)
+        info = plan.run(dev.data_ptr(), _native.make_params(prm), 2, st)
+        print(json.dumps({"case": name, "steps": info.steps, "status": info.status}))
+    elif name == "fdsrc":
+        from astronomix_gb300.time_integration import get_plan
+        from astronomix_gb300.option_classes import (WindConfig, WindParams, TurbulentForcingConfig,
+                                                     TurbulentForcingParams)
+
+        cfg, prm, rv, s = arena_blast(128, "fd")
+        cfg = cfg._replace(wind_config=WindConfig(stellar_wind=True, num_injection_cells=8),
+                           turbulent_forcing_config=TurbulentForcingConfig(turbulent_forcing=True))
+        prm = prm._replace(wind_params=WindParams(wind_mass_loss_rate=1.0, wind_final_velocity=10.0),
+                           turbulent_forcing_params=TurbulentForcingParams(energy_injection_rate=0.2))
         plan = get_plan(cfg, rv, s.shape, np.float32)
         dev = torch.from_numpy(s).cuda()
         st = torch.cuda.current_stream().cuda_stream
