@@ -418,13 +418,7 @@ template <typename T>
 __device__ __forceinline__ bool wind_source(const FDArgs& a, int i, int j, int k, const T* qc, long long nc,
                                             long long c, T dtw, T* src) {
   const double dx = a.dx, half = a.box / 2;
-  // helper_data.r: cell centres dx/2 + i dx, distance from the box centre;
-  // cells whose offset along one axis already exceeds the taper are skipped
-  // before any FP64 arithmetic
-  const float lim = (float)(a.wind_r1 / dx) + 1.0f;
-  const float h = 0.5f * (float)a.n;
-  if (fabsf((float)i + 0.5f - h) > lim || fabsf((float)j + 0.5f - h) > lim || fabsf((float)k + 0.5f - h) > lim)
-    return false;
+  // helper_data.r: cell centres dx/2 + i dx, distance from the box centre
   const double x = dx / 2 + i * dx - half, y = dx / 2 + j * dx - half, z = dx / 2 + k * dx - half;
   const double r = sqrt(x * x + y * y + z * z);
   if (!(r <= a.wind_r1)) return false;
@@ -457,6 +451,10 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
   const T* Ox = b.OB;
   const T* Oy = b.OB + nc;
   const T* Oz = b.OB + 2 * nc;
+  // wind: cells whose offset from the centre along one axis exceeds the taper
+  // (in cells, plus one) are skipped by an FP32 test before any FP64 work
+  const float wlim = a.wind ? (float)(a.wind_r1 / a.dx) + 1.0f : -1.0f;
+  const float wmid = 0.5f * (float)n;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
     decompose(c, n, &i, &j, &k);
@@ -469,7 +467,8 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
     rb[1] = -dtdx * D6(Ox, 2) + dtdx * D6(Oz, 0);
     rb[2] = -dtdx * D6(Oy, 0) + dtdx * D6(Ox, 1);
     T ws[5] = {T(0), T(0), T(0), T(0), T(0)};
-    const bool wind = a.wind && wind_source<T>(a, i, j, k, b.QC, nc, c, k2 * dt, ws);
+    const bool wind = fabsf((float)i + 0.5f - wmid) <= wlim && fabsf((float)j + 0.5f - wmid) <= wlim &&
+                      fabsf((float)k + 0.5f - wmid) <= wlim && wind_source<T>(a, i, j, k, b.QC, nc, c, k2 * dt, ws);
     auto rhs = [&](int r) {
       const T rq = -dtdx * b.ACC[r * nc + c];
       return (wind && r < 5) ? rq + ws[r] : rq;
