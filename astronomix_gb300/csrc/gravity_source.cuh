@@ -238,6 +238,88 @@ __global__ void __launch_bounds__(kGThreads) k_grav_faces(GravSrc<T> a) {
   }
 }
 
+// k_grav_faces for the contiguous (last) axis: the lanes of a warp take 32
+// neighbouring cells of one line (coalesced loads), each the states of its
+// own cell; the interface left of a lane's cell takes the left neighbour's
+// right state by a shuffle, and a cell's right interface share comes from the
+// next lane.  A warp completes the 30 cells of lanes 1 .. 30.
+template <typename T, int DIM, int RS>
+__global__ void __launch_bounds__(kGThreads) k_grav_faces_last(GravSrc<T> a) {
+  constexpr int NV = DIM + 2;
+  constexpr int k = DIM - 1;
+  constexpr int kCells = 30;
+  const FVControl* ctl = a.ctl;
+  if (!*(volatile const int*)&ctl->active) return;
+  const T h = T(*(volatile const double*)&ctl->dt * a.dt_scale);
+  const T gamma = T(a.gamma);
+  const T dxT = T(a.dx);
+  const int n = a.g.n;
+  const long long ntrans = a.nc / n;
+  const int nseg = (n + kCells - 1) / kCells;
+  const long long total = ntrans * nseg;  // warps
+  const int version = a.version;
+  const bool lm = a.lm != 0;
+  const bool rsplit = version == AMX_RIEMANN_SPLIT || version == AMX_RIEMANN_SPLIT_UNSTABLE;
+  const bool unstable = version == AMX_RIEMANN_SPLIT_UNSTABLE;
+  const T alpha = T(((volatile const double*)ctl->seam_maxima)[k]);
+  const int lane = threadIdx.x & 31;
+  const long long warps_per_grid = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < total; w += warps_per_grid) {
+    const long long t = w % ntrans;
+    const int seg = (int)(w / ntrans);
+    int ic[3] = {0, 0, 0};
+    {
+      long long r = t;
+      for (int d = DIM - 2; d >= 0; --d) {
+        ic[d] = (int)(r % n);
+        r /= n;
+      }
+    }
+    // this lane's cell (clamped into the mapped range; lanes past the line end compute unused values)
+    const int jr = seg * kCells - 1 + lane;
+    const int j = jr < n ? jr : n;
+    T qm[NV], q0[NV], qp[NV], lo[NV], hi[NV];
+    grav_load<T, DIM>(a, ic, k, j - 1, qm);
+    grav_load<T, DIM>(a, ic, k, j, q0);
+    grav_load<T, DIM>(a, ic, k, j + 1, qp);
+    grav_states<T, DIM>(a, qm, q0, qp, k, gamma, h, dxT, lo, hi);
+    // interface j - 1/2: the left cell's right state from the previous lane
+    T hiL[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) hiL[v] = __shfl_up_sync(0xffffffffu, hi[v], 1);
+    T to_im1 = T(0), im1 = T(0);
+    if (lane > 0) {
+      if (rsplit) {
+        riemann_split_mass<T, DIM>(hiL, lo, k + 1, gamma, lm, unstable, &to_im1, &im1);
+      } else {
+        T F[NV];
+        riemann<T, DIM, RS>(hiL, lo, k + 1, gamma, alpha, lm, F);
+        if (version == AMX_DONOR_ACCOUNTING) {
+          to_im1 = jmin(F[0], T(0));
+          im1 = jmax(F[0], T(0));
+        } else {  // HALF_SPLIT
+          to_im1 = T(0.5) * F[0];
+          im1 = T(0.5) * F[0];
+        }
+      }
+    }
+    // the share of this cell's right interface, computed by the next lane
+    const T share_r = __shfl_down_sync(0xffffffffu, im1, 1);
+    if (lane >= 1 && lane <= kCells && jr < n) {
+      const T pm = grav_phi(a, ic, k, jr - 1), p0 = grav_phi(a, ic, k, jr), pp = grav_phi(a, ic, k, jr + 1);
+      const T acc_b = -(p0 - pm) / dxT;
+      const T acc_f = -(pp - p0) / dxT;
+      const T e = to_im1 * acc_b + share_r * acc_f;
+      int jc[3] = {ic[0], ic[1], ic[2]};
+      jc[k] = jr;
+      long long c = jc[0];
+      if (DIM >= 2) c = c * n + jc[1];
+      if (DIM >= 3) c = c * n + jc[2];
+      a.eacc[c] = (k == 0) ? e : a.eacc[c] + e;
+    }
+  }
+}
+
 // The update of _apply_self_gravity (_self_gravity.py:341-390), one cell per
 // thread: momentum source rho a_k with the central acceleration
 // a_k = -(phi[i+1] - phi[i-1]) / 2dx, energy source rho v_k a_k summed over
@@ -296,7 +378,18 @@ inline int grav_grid_for(long long work, int num_sms) {
 }
 
 template <typename T, int DIM, int K>
-void grav_faces_axis(const GravSrc<T>& a, int rs, int grid, cudaStream_t s) {
+void grav_faces_axis(const GravSrc<T>& a, int rs, int num_sms, cudaStream_t s) {
+  const long long ntrans = a.nc / a.g.n;
+  if (K == DIM - 1) {
+    // one warp per 30 cells of a line along the contiguous axis
+    const long long warps = ntrans * ((a.g.n + 29) / 30);
+    const int grid = grav_grid_for(warps * 32, num_sms);
+    if (rs == AMX_LAX_FRIEDRICHS) k_grav_faces_last<T, DIM, RS_LF><<<grid, kGThreads, 0, s>>>(a);
+    else if (rs == AMX_HLL) k_grav_faces_last<T, DIM, RS_HLL><<<grid, kGThreads, 0, s>>>(a);
+    else k_grav_faces_last<T, DIM, RS_HLLC><<<grid, kGThreads, 0, s>>>(a);
+    return;
+  }
+  const int grid = grav_grid_for(ntrans * ((a.g.n + kGSeg - 1) / kGSeg), num_sms);
   if (rs == AMX_LAX_FRIEDRICHS) k_grav_faces<T, DIM, RS_LF, K><<<grid, kGThreads, 0, s>>>(a);
   else if (rs == AMX_HLL) k_grav_faces<T, DIM, RS_HLL, K><<<grid, kGThreads, 0, s>>>(a);
   else k_grav_faces<T, DIM, RS_HLLC, K><<<grid, kGThreads, 0, s>>>(a);
@@ -305,11 +398,9 @@ void grav_faces_axis(const GravSrc<T>& a, int rs, int grid, cudaStream_t s) {
 template <typename T, int DIM>
 int grav_source_dim(const GravSrc<T>& a, int rs, int num_sms, cudaStream_t s) {
   if (a.version != AMX_SIMPLE_SOURCE_TERM) {
-    const long long lines = (a.nc / a.g.n) * ((a.g.n + kGSeg - 1) / kGSeg);
-    const int grid = grav_grid_for(lines, num_sms);
-    grav_faces_axis<T, DIM, 0>(a, rs, grid, s);
-    if (DIM >= 2) grav_faces_axis<T, DIM, (DIM >= 2 ? 1 : 0)>(a, rs, grid, s);
-    if (DIM >= 3) grav_faces_axis<T, DIM, (DIM >= 3 ? 2 : 0)>(a, rs, grid, s);
+    grav_faces_axis<T, DIM, 0>(a, rs, num_sms, s);
+    if (DIM >= 2) grav_faces_axis<T, DIM, (DIM >= 2 ? 1 : 0)>(a, rs, num_sms, s);
+    if (DIM >= 3) grav_faces_axis<T, DIM, (DIM >= 3 ? 2 : 0)>(a, rs, num_sms, s);
   }
   k_grav_update<T, DIM><<<grav_grid_for(a.nc, num_sms), kGThreads, 0, s>>>(a);
   return cudaGetLastError() == cudaSuccess ? AMX_OK : AMX_ERR_CUDA;
