@@ -196,6 +196,21 @@ int fv_run_mode(amx_plan* p, void* state, const amx_params* prm, int mode, doubl
   return fv_launch(p, a, s);
 }
 
+// The end of a device-driven step: t += dt, the step count and the history
+// records (when ctl->active).
+__global__ void k_step_advance(FVControl* ctl, double* dt_hist, int* it_hist, long long max_hist, int mhd) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (!ctl->active) return;
+  const double dt = ctl->dt;
+  ctl->t = ctl->t + dt;
+  const long long idx = ctl->steps;
+  ctl->steps = idx + 1;
+  const int it = mhd ? ctl->mag_iters : 0;
+  ctl->mag_iters_total += it;
+  if (dt_hist && idx < max_hist) dt_hist[idx] = dt;
+  if (it_hist && idx < max_hist) it_hist[idx] = it;
+}
+
 // A device-driven seam (dt from ctl->dt times dt_scale; skipped unless ctl->active).
 int fv_seam(amx_plan* p, void* state, const amx_params* prm, int mode, double dt_scale, double t_pause,
             cudaStream_t s) {
@@ -251,7 +266,10 @@ int fv_device_step(amx_plan* p, void* state, const amx_params* prm, double t_pau
     }
   }
   if (rc) return rc;
-  if (!evolve_only) rc = amx::grav_advance(p->ctl, p->dt_hist, p->it_hist, p->max_hist, p->cfg.mhd, s);
+  if (!evolve_only) {
+    k_step_advance<<<1, 32, 0, s>>>(p->ctl, p->dt_hist, p->it_hist, p->max_hist, p->cfg.mhd);
+    rc = cuda_ok(cudaGetLastError());
+  }
   return rc;
 }
 

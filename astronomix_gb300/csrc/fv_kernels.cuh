@@ -1339,18 +1339,23 @@ fv_run_kernel(FVArgs<T> a) {
     }
     return;
   }
-  // the seams need the maxima of the state they start from (Lax-Friedrichs alpha)
+  // the seams need the maxima of the state they start from only for the
+  // Lax-Friedrichs alpha and the VAN_ALBADA_PP weights
+  constexpr bool seam_maxima = (RS == RS_LF) || pp;
   if (a.mode == FV_MODE_HYDRO_RK2) {
     double dt_in = a.dt_in;
     if (a.dt_dev) {
       if (!*(volatile int*)&ctl->active) return;
       dt_in = *(volatile double*)&ctl->dt;
     }
-    if (!cfl_phase()) return;
-    if (a.dt_dev && blockIdx.x == 0 && threadIdx.x == 0) {
-      double m[3];
-      last_maxima(m);
-      for (int k = 0; k < 3; ++k) ctl->seam_maxima[k] = m[k];
+    if (seam_maxima) {
+      if (!cfl_phase()) return;
+      // the gravity source term's Lax-Friedrichs alpha (the old state's maxima)
+      if (a.dt_dev && blockIdx.x == 0 && threadIdx.x == 0) {
+        double m[3];
+        last_maxima(m);
+        for (int k = 0; k < 3; ++k) ctl->seam_maxima[k] = m[k];
+      }
     }
     rk2(T(dt_in * a.dt_scale), false);
     return;
@@ -1372,7 +1377,7 @@ fv_run_kernel(FVArgs<T> a) {
       if (!*(volatile int*)&ctl->active) return;
       dt_in = *(volatile double*)&ctl->dt;
     }
-    if (!cfl_phase()) return;
+    if (seam_maxima && !cfl_phase()) return;
     const T dtT = T(dt_in);
     if (MHD) {
       if (!rk2(dtT / T(2), false)) return;

@@ -247,18 +247,6 @@ __global__ void k_crop(const T* __restrict__ fout, GravGrid g, T* __restrict__ o
   }
 }
 
-__global__ void k_grav_advance(FVControl* ctl, double* dt_hist, int* it_hist, long long max_hist, int mhd) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (!ctl->active) return;
-  const double dt = ctl->dt;
-  ctl->t = ctl->t + dt;
-  const long long idx = ctl->steps;
-  ctl->steps = idx + 1;
-  const int it = mhd ? ctl->mag_iters : 0;
-  ctl->mag_iters_total += it;
-  if (dt_hist && idx < max_hist) dt_hist[idx] = dt;
-  if (it_hist && idx < max_hist) it_hist[idx] = it;
-}
 
 inline int cuda_ok(cudaError_t e) { return e == cudaSuccess ? AMX_OK : AMX_ERR_CUDA; }
 inline int fft_ok(cufftResult r) { return r == CUFFT_SUCCESS ? AMX_OK : AMX_ERR_CUDA; }
@@ -557,10 +545,6 @@ int grav_apply(GravPlan* p, const void* old_state, void* state, const FVControl*
   return apply_t<double>(p, static_cast<const double*>(old_state), static_cast<double*>(state), ctl, dt_scale, prm, s);
 }
 
-int grav_advance(FVControl* ctl, double* dt_hist, int* it_hist, long long max_hist, int mhd, cudaStream_t s) {
-  k_grav_advance<<<1, 32, 0, s>>>(ctl, dt_hist, it_hist, max_hist, mhd);
-  return cuda_ok(cudaGetLastError());
-}
 
 }  // namespace amx
 

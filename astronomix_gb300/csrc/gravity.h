@@ -29,8 +29,4 @@ void* grav_old_state(GravPlan* g);
 int grav_apply(GravPlan* g, const void* old_state, void* state, const FVControl* ctl, double dt_scale,
                const amx_params& prm, cudaStream_t s);
 
-// The end of a device-driven step: t += dt, step count, history records
-// (when ctl->active).
-int grav_advance(FVControl* ctl, double* dt_hist, int* it_hist, long long max_hist, int mhd, cudaStream_t s);
-
 }  // namespace amx
