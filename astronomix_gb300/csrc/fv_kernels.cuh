@@ -116,7 +116,7 @@ template <typename T> struct Tile<T, 1> {
   static constexpr int T0 = 256, T1 = 1, T2 = 1;
 };
 template <> struct Tile<float, 2> {
-  static constexpr int T0 = 8, T1 = 64, T2 = 1;
+  static constexpr int T0 = 16, T1 = 32, T2 = 1;
 };
 template <> struct Tile<double, 2> {
   static constexpr int T0 = 4, T1 = 64, T2 = 1;
@@ -135,7 +135,7 @@ template <typename T> struct TileV<T, 2, 1> {
   static constexpr int T0 = 4, T1 = 64, T2 = 1;
 };
 template <typename T> struct TileV<T, 2, 2> {
-  static constexpr int T0 = 16, T1 = 32, T2 = 1;
+  static constexpr int T0 = 8, T1 = 64, T2 = 1;
 };
 
 constexpr int kFVThreads = 256;
