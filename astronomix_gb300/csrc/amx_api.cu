@@ -165,7 +165,7 @@ int fv_prepare(amx_plan* p, cudaStream_t s) {
   // cfl, alpha and mag slots are the leading members of FVControl
   const size_t n = offsetof(FVControl, dt);
   int rc = cuda_ok(cudaMemsetAsync(p->ctl, 0, n, s));
-  rc |= cuda_ok(cudaMemsetAsync(&p->ctl->bar_count, 0, sizeof(unsigned int) * 2 + sizeof(int), s));
+  rc |= cuda_ok(cudaMemsetAsync(&p->ctl->bar_count, 0, sizeof(unsigned long long) + sizeof(int), s));
   return rc;
 }
 

@@ -70,49 +70,49 @@ __device__ __forceinline__ T nanmax(T a, T b) {
 
 // ------------------------------------------------------------ grid barrier
 
-// Sense-free generation barrier for cooperative launches.  Every spin is
-// bounded: after AMX_BARRIER_SPIN_LIMIT polls the block gives up, records
-// AMX_ERR_TIMEOUT and the barrier returns false so the caller can unwind.
-// A block that has seen `abort` set also returns false immediately.
+// Grid barrier for cooperative launches.  Every spin is bounded: after
+// AMX_BARRIER_SPIN_LIMIT polls the block gives up, records AMX_ERR_TIMEOUT
+// and the barrier returns false so the caller can unwind.  A block that has
+// seen `abort` set also returns false immediately.
 struct GridBarrier {
-  unsigned int* count;       // arrivals in the current generation
-  unsigned int* generation;  // incremented by the last arrival
-  int* abort_flag;           // set once any block timed out
+  unsigned long long* count;  // arrivals since the launch began (zeroed before it)
+  int* abort_flag;            // set once any block timed out
 };
 
 #ifndef AMX_BARRIER_SPIN_LIMIT
 #define AMX_BARRIER_SPIN_LIMIT (1u << 24)
 #endif
 
+// Barrier number b of a launch is passed when the arrival counter reaches
+// b * gridDim.x: every block adds one and waits for the multiple of the grid
+// size above the value it drew, so no block resets anything and the last
+// arrival needs no extra round trips.  (No block can arrive at barrier b + 1
+// before all have arrived at b, so the values drawn at b lie in
+// [(b - 1) N, b N).)  64-bit, so the counter cannot wrap within a launch.
 __device__ __forceinline__ bool grid_sync(const GridBarrier& b, int* status) {
   __syncthreads();
   __shared__ int s_ok;
   if (threadIdx.x == 0) {
     int ok = 1;
-    volatile unsigned int* gen = b.generation;
     volatile int* ab = b.abort_flag;
     if (*ab) {
       ok = 0;
     } else {
-      const unsigned int my_gen = *gen;
       __threadfence();
-      const unsigned int arrived = atomicAdd(b.count, 1u);
-      if (arrived == gridDim.x - 1) {
-        atomicExch(b.count, 0u);
-        __threadfence();
-        atomicAdd(b.generation, 1u);
-      } else {
-        unsigned int spins = 0;
-        while (*gen == my_gen) {
-          if (*ab) { ok = 0; break; }
-          if (++spins > AMX_BARRIER_SPIN_LIMIT) {
-            ok = 0;
-            atomicExch(b.abort_flag, 1);
-            raise_status(status, AMX_ERR_TIMEOUT);
-            break;
-          }
-          __nanosleep(64);
+      const unsigned long long n = gridDim.x;
+      const unsigned long long arrived = atomicAdd(b.count, 1ull);
+      const unsigned long long target = (arrived / n + 1ull) * n;
+      volatile unsigned long long* cnt = b.count;
+      unsigned int spins = 0;
+      while (*cnt < target) {
+        if (*ab) { ok = 0; break; }
+        if (++spins > AMX_BARRIER_SPIN_LIMIT) {
+          ok = 0;
+          atomicExch(b.abort_flag, 1);
+          raise_status(status, AMX_ERR_TIMEOUT);
+          break;
         }
+        __nanosleep(32);
       }
       __threadfence();
     }

@@ -56,8 +56,7 @@ __global__ void batch_prepare_kernel(BatchRunCtl* rc, int R, BatchControl* ctl) 
     else rc[r].mag[k - 12] = 0ull;
   }
   if (threadIdx.x == 0) {
-    ctl->bar_count = 0u;
-    ctl->bar_gen = 0u;
+    ctl->bar_count = 0ull;
     ctl->abort_flag = 0;
   }
 }

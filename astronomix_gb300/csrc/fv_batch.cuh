@@ -54,7 +54,7 @@ struct BatchRunCtl {
 };
 
 struct BatchControl {
-  unsigned int bar_count, bar_gen;
+  unsigned long long bar_count;  // grid-barrier arrivals of the current launch
   int abort_flag;
   int status;        // launch-level status (barrier timeout)
   long long passes;  // grid-barrier phases run (all launches)
@@ -148,7 +148,7 @@ fv_batch_kernel(BatchArgs<T> b) {
   BatchControl* ctl = b.ctl;
   BatchRunCtl* rc = b.rctl;
   int* status = &ctl->status;
-  const GridBarrier bar{&ctl->bar_count, &ctl->bar_gen, &ctl->abort_flag};
+  const GridBarrier bar{&ctl->bar_count, &ctl->abort_flag};
   const int R = b.num_runs;
 
   for (int r = threadIdx.x; r < R; r += blockDim.x) {

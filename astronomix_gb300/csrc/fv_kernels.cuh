@@ -38,7 +38,7 @@ struct FVControl {
   int mag_iters;                  // fixed-point iterations of the last magnetic update
   int pad0;
   long long mag_iters_total;
-  unsigned int bar_count, bar_gen;
+  unsigned long long bar_count;   // grid-barrier arrivals of the current launch
   int abort_flag;
   int status;
   // device-driven seams (dt_dev): FV_MODE_DT sets dt and whether a step is
@@ -1141,7 +1141,7 @@ fv_run_kernel(FVArgs<T> a) {
   __shared__ double red[32];
   FVControl* ctl = a.ctl;
   int* status = &ctl->status;
-  const GridBarrier bar{&ctl->bar_count, &ctl->bar_gen, &ctl->abort_flag};
+  const GridBarrier bar{&ctl->bar_count, &ctl->abort_flag};
   const long long nc = a.ncells;
   T* gas = a.state;
   constexpr int NVG_ = DIM + 2;
