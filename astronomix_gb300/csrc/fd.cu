@@ -7,6 +7,7 @@
 // only checks the control block every few steps.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <new>
 
@@ -33,6 +34,8 @@ struct FDPlan {
   unsigned char* ws = nullptr;
   fd::FDLaunch L{};
   double wind_V = 0.0;              // stellar wind: sum of the injection mask x dx^3
+  int wind_lo = 0, wind_n = 0;      // the cube of cells that holds the taper
+  void* wind_src = nullptr;         // [5][wind_n^3] stage source
   ForcingPlan* force = nullptr;     // turbulent forcing (null without)
 };
 
@@ -67,6 +70,8 @@ fd::FDArgs make_args(const FDPlan* p, const amx_params& prm, double t_pause) {
   a.wind_rinj = p->cfg.num_injection_cells * p->cfg.grid_spacing;
   a.wind_r1 = 1.3 * a.wind_rinj;
   a.box = p->cfg.box_size;
+  a.wind_lo = p->wind_lo;
+  a.wind_n = p->wind_n;
   return a;
 }
 
@@ -132,7 +137,19 @@ int fd_plan_create(const amx_config& cfg, int64_t max_history, FDPlan** out) {
   p->L.grid = (int)(want < (long long)sms * 8 ? want : (long long)sms * 8);
   int rc = (cfg.dtype == AMX_F32) ? fd::fd_set_attrs_f32() : fd::fd_set_attrs_f64();
   if (rc || cudaDeviceSynchronize() != cudaSuccess) { cudaFree(p->ws); delete p; return AMX_ERR_CUDA; }
-  if (cfg.stellar_wind) p->wind_V = wind_volume(cfg);
+  if (cfg.stellar_wind) {
+    p->wind_V = wind_volume(cfg);
+    // cells whose centre lies within 1.3 r_inj (plus one cell) of the box centre along every axis
+    const double lim = 1.3 * cfg.num_injection_cells + 1.0;
+    const double mid = 0.5 * cfg.num_cells - 0.5;
+    const int lo = std::max(0, (int)std::floor(mid - lim));
+    const int hi = std::min(cfg.num_cells - 1, (int)std::ceil(mid + lim));
+    p->wind_lo = lo;
+    p->wind_n = hi - lo + 1;
+    const size_t wbytes = (size_t)5 * p->wind_n * p->wind_n * p->wind_n * p->elem;
+    if (cudaMalloc(&p->wind_src, wbytes) != cudaSuccess) { fd_plan_destroy(p); return AMX_ERR_CUDA; }
+    p->L.wind_src = p->wind_src;
+  }
   if (cfg.turbulent_forcing) {
     rc = forcing_plan_create(cfg, &p->force);
     if (rc) { fd_plan_destroy(p); return rc; }
@@ -144,6 +161,7 @@ int fd_plan_create(const amx_config& cfg, int64_t max_history, FDPlan** out) {
 void fd_plan_destroy(FDPlan* p) {
   if (!p) return;
   if (p->force) forcing_plan_destroy(p->force);
+  if (p->wind_src) cudaFree(p->wind_src);
   if (p->ws) cudaFree(p->ws);
   delete p;
 }

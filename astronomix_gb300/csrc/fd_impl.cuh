@@ -48,6 +48,7 @@ struct Bufs {
   T* OM;   // 3  edge EMFs Omega_x, Omega_y, Omega_z (point values)
   T* OB;   // 3  edge EMFs (averages)
   FDControl* ctl;
+  T* WS;   // stellar wind: [5][wind_n^3] source of the current stage
   FDArgs a;
 };
 
@@ -434,6 +435,29 @@ __device__ __forceinline__ bool wind_source(const FDArgs& a, int i, int j, int k
   return true;
 }
 
+// The wind source of one stage over the cube of cells that holds the taper
+// (zero outside it), before k_update adds it to the right-hand side.  Its
+// own kernel, so that the FP64 arithmetic does not weigh on the update's
+// registers.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_wind_source(Bufs<T> b, int stage) {
+  FD_ACTIVE_OR_RETURN(b.ctl);
+  const FDArgs a = b.a;
+  const int n = a.n, wn = a.wind_n, lo = a.wind_lo;
+  const long long nc = a.nc, wn3 = (long long)wn * wn * wn;
+  const T dt = T(*(volatile double*)&b.ctl->dt);
+  const T k2 = T(kRHS[stage]);
+  for (long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x; w < wn3; w += (long long)gridDim.x * blockDim.x) {
+    const int wi = (int)(w / ((long long)wn * wn)), wj = (int)((w / wn) % wn), wk = (int)(w % wn);
+    const int i = lo + wi, j = lo + wj, k = lo + wk;
+    const long long c = cidx(i, j, k, n);
+    T src[5] = {T(0), T(0), T(0), T(0), T(0)};
+    wind_source<T>(a, i, j, k, b.QC, nc, c, k2 * dt, src);
+#pragma unroll
+    for (int r = 0; r < 5; ++r) b.WS[r * wn3 + w] = src[r];
+  }
+}
+
 // RHS and the SSPRK(5,4) combination (_ssprk.py:224-228, :298-310, :328-332)
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
@@ -451,10 +475,8 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
   const T* Ox = b.OB;
   const T* Oy = b.OB + nc;
   const T* Oz = b.OB + 2 * nc;
-  // wind: cells whose offset from the centre along one axis exceeds the taper
-  // (in cells, plus one) are skipped by an FP32 test before any FP64 work
-  const float wlim = a.wind ? (float)(a.wind_r1 / a.dx) + 1.0f : -1.0f;
-  const float wmid = 0.5f * (float)n;
+  const int wlo = a.wind_lo, wn = a.wind ? a.wind_n : 0;
+  const long long wn3 = (long long)wn * wn * wn;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
     decompose(c, n, &i, &j, &k);
@@ -466,9 +488,15 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
     rb[0] = -dtdx * D6(Oz, 1) + dtdx * D6(Oy, 2);
     rb[1] = -dtdx * D6(Ox, 2) + dtdx * D6(Oz, 0);
     rb[2] = -dtdx * D6(Oy, 0) + dtdx * D6(Ox, 1);
+    // the wind source of this stage (k_wind_source), for the cells of the taper's cube
     T ws[5] = {T(0), T(0), T(0), T(0), T(0)};
-    const bool wind = fabsf((float)i + 0.5f - wmid) <= wlim && fabsf((float)j + 0.5f - wmid) <= wlim &&
-                      fabsf((float)k + 0.5f - wmid) <= wlim && wind_source<T>(a, i, j, k, b.QC, nc, c, k2 * dt, ws);
+    const unsigned wi = (unsigned)(i - wlo), wj = (unsigned)(j - wlo), wk = (unsigned)(k - wlo);
+    const bool wind = wi < (unsigned)wn && wj < (unsigned)wn && wk < (unsigned)wn;
+    if (wind) {
+      const long long w = ((long long)wi * wn + wj) * wn + wk;
+#pragma unroll
+      for (int r = 0; r < 5; ++r) ws[r] = b.WS[r * wn3 + w];
+    }
     auto rhs = [&](int r) {
       const T rq = -dtdx * b.ACC[r * nc + c];
       return (wind && r < 5) ? rq + ws[r] : rq;
@@ -544,6 +572,7 @@ Bufs<T> make_bufs(const FDLaunch& L, void* state, const FDArgs& a) {
   T** dst[10] = {&b.Q0, &b.Q, &b.QF, &b.QC, &b.ACC, &b.B, &b.BF, &b.M, &b.OM, &b.OB};
   for (int i = 0; i < 10; ++i) *dst[i] = static_cast<T*>(L.bufs[i]);
   b.ctl = L.ctl;
+  b.WS = static_cast<T*>(L.wind_src);
   b.a = a;
   return b;
 }
@@ -572,6 +601,11 @@ int launch_stages(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t 
     k_weno<T, 2><<<wg, kThreads, wsm, s>>>(b);
     k_emf<T><<<g, kThreads, 0, s>>>(b);
     k_emf_avg<T><<<g, kThreads, 0, s>>>(b);
+    if (a.wind) {
+      const long long wn3 = (long long)a.wind_n * a.wind_n * a.wind_n;
+      const int wg = (int)((wn3 + kThreads - 1) / kThreads < g ? (wn3 + kThreads - 1) / kThreads : g);
+      k_wind_source<T><<<wg, kThreads, 0, s>>>(b, st);
+    }
     k_update<T><<<g, kThreads, 0, s>>>(b, st);
   }
   k_finalize<T><<<g, kThreads, 0, s>>>(b);

@@ -65,6 +65,8 @@ struct FDArgs {
   double wind_rinj;    // injection radius, num_injection_cells dx
   double wind_r1;      // 1.3 x the injection radius (end of the taper)
   double box;          // box size (cell radii from the box centre)
+  int wind_lo;         // the cube of cells that holds the taper: [wind_lo, wind_lo + wind_n) per axis
+  int wind_n;
 };
 
 // buffers and launch geometry handed from the host plan to the typed launchers
@@ -73,6 +75,7 @@ struct FDLaunch {
   int n;
   void* bufs[10];  // Q0 Q QF QC ACC (8 rows) B BF (3) M (6) OM OB (3)
   FDControl* ctl;
+  void* wind_src;  // stellar wind: [5][wind_n^3] source of the current stage (null without)
 };
 
 int fd_set_attrs_f32();
