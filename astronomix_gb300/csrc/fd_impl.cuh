@@ -206,8 +206,11 @@ __device__ __forceinline__ int pmod(int g, int n) {
 }
 
 // Interface fluxes along axis D (0 = x, 1 = y, 2 = z), _weno.py:112-324.
+// One block per SM: the characteristic projection needs about 250 registers
+// per thread; held to 128 (two blocks) it spilled 440 bytes per thread and
+// ran 18 % slower on the 256^3 blast.
 template <typename T, int D>
-__global__ void __launch_bounds__(kThreads, 2) k_weno(Bufs<T> b) {
+__global__ void __launch_bounds__(kThreads, 1) k_weno(Bufs<T> b) {
   FD_ACTIVE_OR_RETURN(b.ctl);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* S = reinterpret_cast<T*>(smem_raw);          // [kAH][kL][kCellVals]
