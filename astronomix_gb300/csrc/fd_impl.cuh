@@ -189,15 +189,23 @@ __global__ void __launch_bounds__(kThreads) k_prep(Bufs<T> b, int stage) {
 
 // ---------------------------------------------------------------- WENO
 
-// 7 cells per tile: its 8 x 32 interfaces are one task per thread
-constexpr int kA = 7;             // cells per tile along the flux axis
-constexpr int kL = 32;            // lanes per tile across it
-constexpr int kAH = kA + 6;       // staged cells along the axis (halo 3)
+// Line tiles of A cells along the flux axis x 32 lanes across it; every
+// staged cell (A + 6 with the halo of 3) costs a flux and an eigensystem, so
+// longer tiles recompute less halo.  One block per SM leaves the shared
+// memory free: FP32 31 cells (the 32 x 32 interfaces are four tasks per
+// thread; 0.083 s against 0.097 s per 256^3 step with 7), FP64 15 cells
+// (what fits in 227 KB).
+template <typename T> struct WenoTile {
+  static constexpr int A = sizeof(T) == 4 ? 31 : 15;  // cells per tile along the flux axis
+  static constexpr int L = 32;                        // lanes per tile across it
+  static constexpr int AH = A + 6;                    // staged cells along the axis (halo 3)
+};
 constexpr int kCellVals = 24;     // U(8) F(8) rho' vx vy vz h (5) cf ca cs (3)
 
 template <typename T>
 constexpr size_t weno_smem() {
-  return sizeof(T) * ((size_t)kAH * kL * kCellVals + (size_t)(kA + 1) * kL * 8);
+  return sizeof(T) * ((size_t)WenoTile<T>::AH * WenoTile<T>::L * kCellVals +
+                      (size_t)(WenoTile<T>::A + 1) * WenoTile<T>::L * 8);
 }
 
 __device__ __forceinline__ int pmod(int g, int n) {
@@ -211,6 +219,7 @@ __device__ __forceinline__ int pmod(int g, int n) {
 // ran 18 % slower on the 256^3 blast.
 template <typename T, int D>
 __global__ void __launch_bounds__(kThreads, 1) k_weno(Bufs<T> b) {
+  constexpr int kA = WenoTile<T>::A, kL = WenoTile<T>::L, kAH = WenoTile<T>::AH;
   FD_ACTIVE_OR_RETURN(b.ctl);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* S = reinterpret_cast<T*>(smem_raw);          // [kAH][kL][kCellVals]
@@ -595,6 +604,7 @@ int launch_stages(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t 
   Bufs<T> b = make_bufs<T>(L, state, a);
   const int g = L.grid;
   const int n = L.n;
+  constexpr int kA = WenoTile<T>::A, kL = WenoTile<T>::L;
   const dim3 wg((n + kA - 1) / kA, (n + kL - 1) / kL, n);
   const size_t wsm = weno_smem<T>();
   for (int st = 0; st < 5; ++st) {
