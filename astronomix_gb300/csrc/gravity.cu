@@ -277,8 +277,8 @@ struct GravPlan {
   void* spec2 = nullptr;  // pruned: the x-transformed half spectrum (spec keeps its planes x >= M zero)
   unsigned char* mem = nullptr;
   size_t bytes = 0;
-  void* fin = nullptr;    // FFT input (E^d real)
-  void* fout = nullptr;   // inverse transform (E^d real): the potential in its solve-grid corner
+  void* fin = nullptr;    // FFT input (E^d real; pruned: the planes x < M, M E^(d-1))
+  void* fout = nullptr;   // inverse transform, same shape: the potential in its solve-grid corner
   void* spec = nullptr;   // half spectrum
   void* kspec = nullptr;  // the Green's function's half spectrum for G = 1, with the inverse
                           // transform's scale: real (periodic) or complex (open)
