@@ -160,13 +160,10 @@ amx::FVArgs<T> make_fv_args(amx_plan* p, void* state, const amx_params* prm, int
   return a;
 }
 
-// zero the reduction slots and the barrier before a cooperative launch
+// zero the reduction slots and the barrier before a cooperative launch (the
+// leading members of FVControl, up to dt)
 int fv_prepare(amx_plan* p, cudaStream_t s) {
-  // cfl, alpha and mag slots are the leading members of FVControl
-  const size_t n = offsetof(FVControl, dt);
-  int rc = cuda_ok(cudaMemsetAsync(p->ctl, 0, n, s));
-  rc |= cuda_ok(cudaMemsetAsync(&p->ctl->bar_count, 0, sizeof(unsigned long long) + sizeof(int), s));
-  return rc;
+  return cuda_ok(cudaMemsetAsync(p->ctl, 0, offsetof(FVControl, dt), s));
 }
 
 template <typename T>

@@ -29,18 +29,22 @@ namespace amx {
 
 // Control block in device memory (one per plan).
 struct FVControl {
+  // zeroed before every launch (one memset up to `dt`)
   unsigned long long red[3][4];   // [slot][axis] maxima of |u_a| + c of a state a phase wrote
   unsigned long long spare[3][4];
   unsigned long long mag[3];      // [slot] fixed-point residual
+  unsigned long long bar_count;   // grid-barrier arrivals of the current launch
+  int abort_flag;
+  int pad_b;
+  // kept across launches
   double dt;                      // dt of the last step taken
   double t;                       // simulation time
   long long steps;                // steps taken
   int mag_iters;                  // fixed-point iterations of the last magnetic update
   int pad0;
   long long mag_iters_total;
-  unsigned long long bar_count;   // grid-barrier arrivals of the current launch
-  int abort_flag;
   int status;
+  int pad2;
   // device-driven seams (dt_dev): FV_MODE_DT sets dt and whether a step is
   // taken; the hydro seam records the maxima of |u_a| + c of its input state
   int active;

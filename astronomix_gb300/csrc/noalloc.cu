@@ -133,8 +133,6 @@ int launch(const amx_config* c, void* state, const amx_params* prm, int64_t max_
     a.max_steps = (max_steps - done < chunk) ? (max_steps - done) : chunk;
     // reduction slots and the barrier start at zero in every launch
     if (cudaMemsetAsync(a.ctl, 0, offsetof(amx::FVControl, dt), s) != cudaSuccess) return AMX_ERR_CUDA;
-    if (cudaMemsetAsync(&a.ctl->bar_count, 0, sizeof(unsigned long long) + sizeof(int), s) != cudaSuccess)
-      return AMX_ERR_CUDA;
     void* args[] = {&a};
     if (cudaLaunchCooperativeKernel(kinfo.fn, dim3(grid), dim3(amx::kFVThreads), args, kinfo.smem, s) !=
         cudaSuccess)
