@@ -230,3 +230,46 @@ def test_evrard_collapse_energy_budget_fp32(cuda):
     assert eg[0] < 0 and ek[0] < 1e-15  # (|u| carries the reference's 1e-20 under the root)
     assert ek[-1] > 1e-3 * abs(eg[0]) and eg[-1] < eg[0], (eg, ek)
     assert abs(et[-1] - et[0]) < 0.02 * abs(eg[0]), (et, eg, ek)
+
+
+def test_split_mhd_fp64(cuda):
+    """Self-gravity after both gas half-updates of the Pang-Wu split with the
+    split MUSCL-Hancock scheme."""
+    cfg, prm, rv, s = grav_case(2, 24, version=DONOR_ACCOUNTING, riemann=HLLC, mhd=True, split=True)
+    got, ref, rec = run_both(cfg, prm, rv, s)
+    assert rec["steps"] >= 4
+    assert rel_err(got, ref) < TOL
+
+
+def test_fixed_timestep_fp64(cuda):
+    cfg, prm, rv, s = grav_case(2, 24, version=HALF_SPLIT, riemann=HLL)
+    cfg = cfg._replace(fixed_timestep=True, num_timesteps=7)
+    got, ref, rec = run_both(cfg, prm, rv, s)
+    assert rec["steps"] == 7
+    assert rel_err(got, ref) < TOL
+
+
+def test_step_seams_with_gravity_fp64(cuda):
+    """amx_evolve_state and amx_fv_hydro_rk2 include the source term, as
+    _evolve_state_fv and _evolve_gas_state_unsplit do."""
+    import torch
+    from astronomix_gb300.time_integration import get_plan
+    from oracle import fv as ofv
+
+    cfg, prm, rv, s = grav_case(2, 16, version=DONOR_ACCOUNTING, riemann=HLL, roll=True)
+    plan = get_plan(cfg, rv, s.shape, np.float64)
+    dev = torch.from_numpy(s.copy()).cuda()
+    st = torch.cuda.current_stream().cuda_stream
+    plan.reset(st)
+    dt = 2e-3
+    plan.evolve(dev.data_ptr(), _native.make_params(prm), dt, st)
+    torch.cuda.synchronize()
+    ref = ofv.evolve_state_fv(s.copy(), np.float64(dt), np.float64(prm.gamma), cfg, rv,
+                              G=prm.gravitational_constant)
+    assert rel_err(dev.cpu().numpy(), ref) < TOL
+    # the gas-update seam: the RK2 update followed by the source term
+    dev2 = torch.from_numpy(s.copy()).cuda()
+    plan.hydro_rk2(dev2.data_ptr(), _native.make_params(prm), dt, st)
+    torch.cuda.synchronize()
+    ref2 = ofv.evolve_gas(s.copy(), np.float64(dt), np.float64(prm.gamma), cfg, rv, G=prm.gravitational_constant)
+    assert rel_err(dev2.cpu().numpy(), ref2) < TOL

@@ -100,3 +100,18 @@ def test_forcing_rejected_with_ghost_cells(cuda):
     cfg, prm = with_forcing(cfg, prm)
     with pytest.raises(ValueError):
         amx.time_integration(s.copy(), cfg, prm, rv)
+
+
+def test_fv_forcing_with_snapshot_pauses_fp64(cuda):
+    """Pausing at snapshot times (amx_run_until on the device-driven steps)
+    leaves the forced run's result unchanged."""
+    from astronomix_gb300 import SnapshotSettings
+
+    cfg, prm, rv, s = smooth_random(3, 12, seed=5, riemann=HLLC, roll=True, t_end=0.012)
+    cfg, prm = with_forcing(cfg, prm, edot=5.0)
+    ref = odriver.time_integration(s.copy(), cfg, prm, rv, time_mode="float64")
+    cfg = cfg._replace(return_snapshots=True, num_snapshots=3,
+                       snapshot_settings=SnapshotSettings(return_final_state=True, return_total_energy=True))
+    snap = amx.time_integration(s.copy(), cfg, prm, rv)
+    assert rel_err(snap.final_state, ref) < TOL
+    assert snap.num_iterations >= 3
