@@ -192,11 +192,11 @@ __global__ void __launch_bounds__(kThreads) k_prep(Bufs<T> b, int stage) {
 // Line tiles of A cells along the flux axis x 32 lanes across it; every
 // staged cell (A + 6 with the halo of 3) costs a flux and an eigensystem, so
 // longer tiles recompute less halo.  One block per SM leaves the shared
-// memory free: FP32 31 cells (the 32 x 32 interfaces are four tasks per
-// thread; 0.083 s against 0.097 s per 256^3 step with 7), FP64 15 cells
-// (what fits in 227 KB).
+// memory free: FP32 47 cells (212 KB; the 48 x 32 interfaces are six tasks
+// per thread; 256^3 step 0.097 s with 7 cells, 0.087 with 15, 0.084 with 31,
+// 0.082 with 47), FP64 15 cells (what fits in 227 KB).
 template <typename T> struct WenoTile {
-  static constexpr int A = sizeof(T) == 4 ? 31 : 15;  // cells per tile along the flux axis
+  static constexpr int A = sizeof(T) == 4 ? 47 : 15;  // cells per tile along the flux axis
   static constexpr int L = 32;                        // lanes per tile across it
   static constexpr int AH = A + 6;                    // staged cells along the axis (halo 3)
 };
