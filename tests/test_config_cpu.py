@@ -52,3 +52,49 @@ def test_make_amx_config_translation():
     assert list(c.bc_lo)[:2] == [P, OPEN_BOUNDARY] and list(c.bc_hi)[:2] == [P, OPEN_BOUNDARY]
     assert c.dtype == 0 and c.grid_spacing == pytest.approx(2.0 / 32)
     assert make_amx_config(cfg, rv, (7, 32, 32), np.float64).dtype == 1
+
+
+def test_physics_switches_reach_the_c_structs():
+    """self-gravity, the wind and the forcing: config and params fields land in
+    amx_config / amx_params, and the limiter rewrite of finalize_config."""
+    from astronomix_gb300 import SimulationParams, VAN_ALBADA, MINMOD, RIEMANN_SPLIT, _native
+    from astronomix_gb300.option_classes import (WindConfig, WindParams, TurbulentForcingConfig,
+                                                 TurbulentForcingParams)
+
+    P = PERIODIC_BOUNDARY
+    per = BoundarySettings(*[BoundarySettings1D(P, P)] * 3)
+    cfg = finalize_config(SimulationConfig(dimensionality=3, self_gravity=True, self_gravity_version=RIEMANN_SPLIT,
+                                           limiter=VAN_ALBADA, boundary_settings=per), (5, 8, 8, 8))
+    assert cfg.limiter == MINMOD  # simulation_config.py:384-389
+    c = make_amx_config(cfg, get_registered_variables(cfg), (5, 8, 8, 8), np.float32)
+    assert c.self_gravity == 1 and c.self_gravity_version == RIEMANN_SPLIT
+    cfg = SimulationConfig(dimensionality=3, mhd=True, solver_mode=FINITE_DIFFERENCE, boundary_settings=per,
+                           wind_config=WindConfig(stellar_wind=True, num_injection_cells=6),
+                           turbulent_forcing_config=TurbulentForcingConfig(turbulent_forcing=True))
+    cfg = finalize_config(cfg, (11, 8, 8, 8))
+    c = make_amx_config(cfg, get_registered_variables(cfg), (11, 8, 8, 8), np.float64)
+    assert (c.stellar_wind, c.num_injection_cells, c.turbulent_forcing) == (1, 6, 1)
+    prm = SimulationParams(gravitational_constant=3.0,
+                           wind_params=WindParams(wind_mass_loss_rate=2.0, wind_final_velocity=5.0),
+                           turbulent_forcing_params=TurbulentForcingParams(energy_injection_rate=0.7))
+    p = _native.make_params(prm)
+    assert (p.gravitational_constant, p.wind_mass_loss_rate, p.wind_final_velocity, p.energy_injection_rate,
+            p.forcing_seed) == (3.0, 2.0, 5.0, 0.7, 42)
+
+
+def test_unsupported_physics_raise_before_any_gpu_work():
+    from astronomix_gb300.time_integration import _check_supported
+    from astronomix_gb300.option_classes import WindConfig, TurbulentForcingConfig
+
+    P = PERIODIC_BOUNDARY
+    per = BoundarySettings(*[BoundarySettings1D(P, P)] * 3)
+    with pytest.raises(NotImplementedError):  # the FV wind is the physics-module injection
+        _check_supported(SimulationConfig(dimensionality=3, wind_config=WindConfig(stellar_wind=True)))
+    with pytest.raises(NotImplementedError):  # self-gravity is an FV feature
+        _check_supported(SimulationConfig(dimensionality=3, mhd=True, solver_mode=FINITE_DIFFERENCE,
+                                          self_gravity=True, boundary_settings=per))
+    with pytest.raises(ValueError):  # the forcing field has the unpadded grid's shape
+        _check_supported(SimulationConfig(dimensionality=3,
+                                          turbulent_forcing_config=TurbulentForcingConfig(turbulent_forcing=True)))
+    _check_supported(SimulationConfig(dimensionality=3, boundary_handling=PERIODIC_ROLL, boundary_settings=per,
+                                      turbulent_forcing_config=TurbulentForcingConfig(turbulent_forcing=True)))
