@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-run batched ensemble")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 128^3 adjoint workload")
     ap.add_argument("--no-gravity", action="store_true", help="skip the self-gravity collapse workload")
-    ap.add_argument("--case", default=None, choices=["fd", "fdsrc", "fv3d", "ensemble", "adjoint", "gravity"],
+    ap.add_argument("--case", default=None, choices=["fd", "fdsrc", "fv3d", "fvsplit", "ensemble", "adjoint",
+                                                     "gravity"],
                     help="run one small case of a secondary workload and exit (for profilers)")
     return ap.parse_args()
 
@@ -59,7 +60,8 @@ def parse():
 def run_case(name):
     """Small, self-contained runs of the secondary workloads for ncu captures:
     fd: FD WENO-CT blast 128^3 FP32, 2 steps; fv3d: FV Lax-Friedrichs MHD
-    blast 192^3 FP32, 2 steps (one launch); ensemble: 8 turbulent 2D MHD
+    blast 192^3 FP32, 2 steps (one launch); fvsplit: the same blast with the
+    split MUSCL-Hancock scheme and HLLC; ensemble: 8 turbulent 2D MHD
     runs (128^2..512^2, t_end / 8) in one batched launch; adjoint: the 3D
     density-perturbation problem at 96^3 to t = 0.01, forward and backward
     with the stored tape (a 4 GB tape budget: the case holds a few GB at
@@ -69,10 +71,10 @@ def run_case(name):
     import torch
     from astronomix_gb300 import _native
 
-    if name in ("fd", "fv3d"):
+    if name in ("fd", "fv3d", "fvsplit"):
         from astronomix_gb300.time_integration import get_plan
 
-        cfg, prm, rv, s = arena_blast(128 if name == "fd" else 192, name[:2])
+        cfg, prm, rv, s = arena_blast(128 if name == "fd" else 192, "fv_split" if name == "fvsplit" else name[:2])
         plan = get_plan(cfg, rv, s.shape, np.float32)
         dev = torch.from_numpy(s).cuda()
         st = torch.cuda.current_stream().cuda_stream
