@@ -113,6 +113,9 @@ _I64 = ctypes.c_int64
 SIGNATURES = {
     "amx_plan_create": (_I32, [ctypes.POINTER(amx_config), _I64, ctypes.POINTER(_P)]),
     "amx_plan_destroy": (_I32, [_P]),
+    "amx_plan_set_limits": (_I32, [_P, _I32, _I64]),
+    "amx_plan_profile": (_I32, [_P, _I32]),
+    "amx_plan_profile_read": (_I32, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), _I32, _I32]),
     "amx_plan_workspace_bytes": (_I32, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     "amx_plan_reset": (_I32, [_P, _P]),
     "amx_plan_set_time": (_I32, [_P, _D, _P]),
@@ -223,6 +226,26 @@ class Plan:
         n = ctypes.c_size_t()
         check(self._L.amx_plan_workspace_bytes(self.handle, ctypes.byref(n)))
         return n.value
+
+    def set_limits(self, max_fixed_point_iterations=0, barrier_spin_limit=0):
+        """Fixed-point cap and grid-barrier poll limit of the FV kernel (0: default)."""
+        check(self._L.amx_plan_set_limits(self.handle, int(max_fixed_point_iterations), int(barrier_spin_limit)),
+              "amx_plan_set_limits")
+
+    FD_KERNELS = ("cfl", "prep", "weno_x", "weno_y", "weno_z", "emf", "emf_avg", "wind", "update", "finalize",
+                  "forcing")
+
+    def profile(self, enable=True):
+        """Per-kernel CUDA-event timing of the FD step (FD plans only)."""
+        check(self._L.amx_plan_profile(self.handle, int(bool(enable))), "amx_plan_profile")
+
+    def profile_read(self, reset=True):
+        """{kernel kind: (total ms, launches)} since the last reset."""
+        n = len(self.FD_KERNELS)
+        ms = (ctypes.c_double * n)()
+        ln = (ctypes.c_int64 * n)()
+        check(self._L.amx_plan_profile_read(self.handle, ms, ln, n, int(bool(reset))), "amx_plan_profile_read")
+        return {k: (ms[i], ln[i]) for i, k in enumerate(self.FD_KERNELS)}
 
     def reset(self, stream=0):
         check(self._L.amx_plan_reset(self.handle, _P(stream)), "amx_plan_reset")

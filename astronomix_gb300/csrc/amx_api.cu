@@ -15,6 +15,7 @@
 #include "fv_registry.h"
 #include "forcing.h"
 #include "gravity.h"
+#include "validate.h"
 
 extern "C" int amx_diag_sums_raw(const amx_config* cfg, const void* state, double gamma, double* out_dev,
                                  void* stream);
@@ -43,6 +44,9 @@ struct amx_plan {
   double* diag = nullptr;   // 8 doubles of reduction scratch for amx_conservation_sums
   // FD
   amx::FDPlan* fd = nullptr;
+  // limits of the persistent kernel (amx_plan_set_limits)
+  int max_iters = 1000;                                    // the reference's fixed-point cap
+  unsigned long long spin_limit = AMX_BARRIER_SPIN_LIMIT;  // polls per grid barrier
   // FV self-gravity and turbulent forcing (null without)
   amx::GravPlan* grav = nullptr;
   amx::ForcingPlan* force = nullptr;
@@ -53,63 +57,6 @@ namespace {
 inline int cuda_ok(cudaError_t e) { return e == cudaSuccess ? AMX_OK : AMX_ERR_CUDA; }
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-int validate(const amx_config* c) {
-  if (!c) return AMX_ERR_INVALID_ARG;
-  if (c->dtype != AMX_F32 && c->dtype != AMX_F64) return AMX_ERR_INVALID_ARG;
-  if (c->dimensionality < 1 || c->dimensionality > 3) return AMX_ERR_INVALID_ARG;
-  if (c->num_cells < 4) return AMX_ERR_INVALID_ARG;
-  if (!(c->grid_spacing > 0.0)) return AMX_ERR_INVALID_ARG;
-  if (c->solver_mode == AMX_FINITE_VOLUME) {
-    const int nv = c->dimensionality + 2 + (c->mhd ? 3 : 0);
-    if (c->num_vars != nv) return AMX_ERR_INVALID_ARG;
-    if (c->mhd && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
-    if (c->split != 0 && c->split != 1) return AMX_ERR_INVALID_ARG;
-    if (c->riemann_solver < AMX_HLL || c->riemann_solver > AMX_LAX_FRIEDRICHS) return AMX_ERR_UNSUPPORTED;
-    if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA_PP) return AMX_ERR_UNSUPPORTED;
-    // the reference's 1D VAN_ALBADA_PP sums its velocity terms over the whole grid
-    if (c->limiter == AMX_VAN_ALBADA_PP && !c->split && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
-    // FV wind injection (the physics-module path) is not part of this library
-    if (c->stellar_wind) return AMX_ERR_UNSUPPORTED;
-    // the forcing field has the unpadded grid's shape (_turbulent_forcing.py:30-40):
-    // 3D with periodic roll, as in the reference
-    if (c->turbulent_forcing && (c->dimensionality != 3 || c->boundary_handling != AMX_PERIODIC_ROLL))
-      return AMX_ERR_UNSUPPORTED;
-    if (c->self_gravity) {
-      if (c->self_gravity_version < AMX_SIMPLE_SOURCE_TERM || c->self_gravity_version > AMX_HALF_SPLIT)
-        return AMX_ERR_INVALID_ARG;
-      // the reference sets MINMOD for self-gravity (simulation_config.py:384-389);
-      // the source term reconstructs with any limited-linear limiter, not VAN_ALBADA_PP
-      if (c->limiter == AMX_VAN_ALBADA_PP) return AMX_ERR_UNSUPPORTED;
-      // _self_gravity.py:163-167: the Riemann-split versions are HLLC-only
-      if ((c->self_gravity_version == AMX_RIEMANN_SPLIT || c->self_gravity_version == AMX_RIEMANN_SPLIT_UNSTABLE) &&
-          c->riemann_solver != AMX_HLLC && c->riemann_solver != AMX_HLLC_LM)
-        return AMX_ERR_UNSUPPORTED;
-    }
-    if (c->boundary_handling == AMX_GHOST_CELLS) {
-      for (int k = 0; k < c->dimensionality; ++k) {
-        for (int side = 0; side < 2; ++side) {
-          const int b = side ? c->bc_hi[k] : c->bc_lo[k];
-          if (b != AMX_BC_OPEN && b != AMX_BC_PERIODIC && b != AMX_BC_REFLECTIVE) return AMX_ERR_UNSUPPORTED;
-          // reflective magnetic/velocity fills of the reference flip the wrong
-          // component for 3-vectors; MHD runs are limited to open / periodic
-          if (c->mhd && b == AMX_BC_REFLECTIVE) return AMX_ERR_UNSUPPORTED;
-        }
-        // periodic must be set on both sides (boundaries.py:105-111)
-        if ((c->bc_lo[k] == AMX_BC_PERIODIC) != (c->bc_hi[k] == AMX_BC_PERIODIC)) return AMX_ERR_UNSUPPORTED;
-      }
-    }
-    return AMX_OK;
-  }
-  if (c->solver_mode == AMX_FINITE_DIFFERENCE) {
-    if (c->dimensionality != 3 || !c->mhd) return AMX_ERR_UNSUPPORTED;
-    if (c->self_gravity) return AMX_ERR_UNSUPPORTED;
-    if (c->num_vars != 11) return AMX_ERR_INVALID_ARG;
-    if (c->num_cells < 8) return AMX_ERR_INVALID_ARG;
-    return AMX_OK;
-  }
-  return AMX_ERR_INVALID_ARG;
-}
 
 long long ipow(long long b, int e) {
   long long r = 1;
@@ -148,7 +95,8 @@ amx::FVArgs<T> make_fv_args(amx_plan* p, void* state, const amx_params* prm, int
   a.dt_in = 0.0;
   a.dt_scale = 1.0;
   a.tol = (c.numerical_precision == 1) ? 1e-10 : 1e-5;
-  a.max_iters = 1000;
+  a.max_iters = p->max_iters;
+  a.spin_limit = p->spin_limit;
   a.mhd = c.mhd;
   a.split = c.split;
   a.first_order = c.first_order_fallback;
@@ -281,7 +229,7 @@ const char* amx_version(void) { return "amx 0.1.0 (sm_103a)"; }
 int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out) {
   if (!out) return AMX_ERR_INVALID_ARG;
   *out = nullptr;
-  int rc = validate(cfg);
+  int rc = amx::validate_config(cfg);
   if (rc) return rc;
   if (max_history < 0) return AMX_ERR_INVALID_ARG;
   amx_plan* p = new (std::nothrow) amx_plan();
@@ -372,6 +320,26 @@ int amx_plan_destroy(amx_plan* p) {
   if (p->ws) cudaFree(p->ws);
   delete p;
   return AMX_OK;
+}
+
+int amx_plan_set_limits(amx_plan* p, int32_t max_fixed_point_iterations, int64_t barrier_spin_limit) {
+  if (!p || max_fixed_point_iterations < 0 || barrier_spin_limit < 0) return AMX_ERR_INVALID_ARG;
+  if (p->fd) return AMX_ERR_UNSUPPORTED;  // the FD step has no fixed point and no grid barrier
+  p->max_iters = max_fixed_point_iterations ? max_fixed_point_iterations : 1000;
+  p->spin_limit = barrier_spin_limit ? (unsigned long long)barrier_spin_limit : AMX_BARRIER_SPIN_LIMIT;
+  return AMX_OK;
+}
+
+int amx_plan_profile(amx_plan* p, int32_t enable) {
+  if (!p) return AMX_ERR_INVALID_ARG;
+  if (!p->fd) return AMX_ERR_UNSUPPORTED;
+  return amx::fd_profile(p->fd, enable != 0);
+}
+
+int amx_plan_profile_read(amx_plan* p, double* ms, int64_t* launches, int32_t n, int32_t reset) {
+  if (!p || n < 0) return AMX_ERR_INVALID_ARG;
+  if (!p->fd) return AMX_ERR_UNSUPPORTED;
+  return amx::fd_profile_read(p->fd, ms, launches, n, reset);
 }
 
 int amx_plan_workspace_bytes(const amx_plan* p, size_t* bytes) {

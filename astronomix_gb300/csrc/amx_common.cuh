@@ -68,20 +68,29 @@ __device__ __forceinline__ T nanmax(T a, T b) {
   return (a != a) ? a : ((b != b) ? b : (b > a ? b : a));
 }
 
+// jnp.minimum: a NaN in either operand wins (fmin would drop it, and a NaN
+// dt would then turn into a finite one)
+template <typename T>
+__device__ __forceinline__ T nanmin(T a, T b) {
+  return (a != a) ? a : ((b != b) ? b : (b < a ? b : a));
+}
+
 // ------------------------------------------------------------ grid barrier
 
 // Grid barrier for cooperative launches.  Every spin is bounded: after
-// AMX_BARRIER_SPIN_LIMIT polls the block gives up, records AMX_ERR_TIMEOUT
-// and the barrier returns false so the caller can unwind.  A block that has
-// seen `abort` set also returns false immediately.
+// `spin_limit` polls (AMX_BARRIER_SPIN_LIMIT unless the plan sets another)
+// the block gives up, records AMX_ERR_TIMEOUT and the barrier returns false
+// so the caller can unwind.  A block that has seen `abort` set also returns
+// false immediately.
+#ifndef AMX_BARRIER_SPIN_LIMIT
+#define AMX_BARRIER_SPIN_LIMIT (1ull << 24)
+#endif
+
 struct GridBarrier {
   unsigned long long* count;  // arrivals since the launch began (zeroed before it)
   int* abort_flag;            // set once any block timed out
+  unsigned long long spin_limit = AMX_BARRIER_SPIN_LIMIT;
 };
-
-#ifndef AMX_BARRIER_SPIN_LIMIT
-#define AMX_BARRIER_SPIN_LIMIT (1u << 24)
-#endif
 
 // Barrier number b of a launch is passed when the arrival counter reaches
 // b * gridDim.x: every block adds one and waits for the multiple of the grid
@@ -103,10 +112,10 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b, int* status) {
       const unsigned long long arrived = atomicAdd(b.count, 1ull);
       const unsigned long long target = (arrived / n + 1ull) * n;
       volatile unsigned long long* cnt = b.count;
-      unsigned int spins = 0;
+      unsigned long long spins = 0;
       while (*cnt < target) {
         if (*ab) { ok = 0; break; }
-        if (++spins > AMX_BARRIER_SPIN_LIMIT) {
+        if (++spins > b.spin_limit) {
           ok = 0;
           atomicExch(b.abort_flag, 1);
           raise_status(status, AMX_ERR_TIMEOUT);

@@ -115,6 +115,7 @@ amx::BatchArgs<T> make_args(const amx_batch* b, const amx_params* prm, long long
   a.base.C_cfl = prm->C_cfl;
   a.base.tol = (c.numerical_precision == 1) ? 1e-10 : 1e-5;
   a.base.max_iters = 1000;
+  a.base.spin_limit = AMX_BARRIER_SPIN_LIMIT;
   a.base.t_pause = INFINITY;
   a.runs = b->d_desc;
   a.rctl = b->d_rctl;

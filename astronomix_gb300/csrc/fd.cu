@@ -37,6 +37,14 @@ struct FDPlan {
   int wind_lo = 0, wind_n = 0;      // the cube of cells that holds the taper
   void* wind_src = nullptr;         // [5][wind_n^3] stage source
   ForcingPlan* force = nullptr;     // turbulent forcing (null without)
+  // per-kernel timing (amx_plan_profile): events after every launch of a step
+  bool profile = false;
+  cudaEvent_t ev_start = nullptr;
+  cudaEvent_t marks[fd::kFDMaxMarks] = {};
+  int marks_kind[fd::kFDMaxMarks] = {};
+  int marks_used = 0;
+  double prof_ms[fd::FD_PH_COUNT] = {};
+  long long prof_launches[fd::FD_PH_COUNT] = {};
 };
 
 namespace {
@@ -99,14 +107,43 @@ double wind_volume(const amx_config& c) {
   return sum * std::pow(dx, 3);
 }
 
-int stages(FDPlan* p, void* state, const fd::FDArgs& a, cudaStream_t s) {
-  return p->cfg.dtype == AMX_F32 ? fd::fd_launch_stages_f32(p->L, state, a, s)
-                                 : fd::fd_launch_stages_f64(p->L, state, a, s);
+int stages(FDPlan* p, const fd::FDLaunch& L, void* state, const fd::FDArgs& a, cudaStream_t s) {
+  return p->cfg.dtype == AMX_F32 ? fd::fd_launch_stages_f32(L, state, a, s)
+                                 : fd::fd_launch_stages_f64(L, state, a, s);
 }
 
-int cfl(FDPlan* p, const void* state, const fd::FDArgs& a, cudaStream_t s) {
-  return p->cfg.dtype == AMX_F32 ? fd::fd_launch_cfl_f32(p->L, state, a, s)
-                                 : fd::fd_launch_cfl_f64(p->L, state, a, s);
+int cfl(FDPlan* p, const fd::FDLaunch& L, const void* state, const fd::FDArgs& a, cudaStream_t s) {
+  return p->cfg.dtype == AMX_F32 ? fd::fd_launch_cfl_f32(L, state, a, s)
+                                 : fd::fd_launch_cfl_f64(L, state, a, s);
+}
+
+// the launch set of one step: with timing on, events after every launch
+fd::FDLaunch step_launch(FDPlan* p, cudaStream_t s) {
+  fd::FDLaunch L = p->L;
+  if (p->profile) {
+    p->marks_used = 0;
+    cudaEventRecord(p->ev_start, s);
+    L.marks = p->marks;
+    L.marks_kind = p->marks_kind;
+    L.marks_used = &p->marks_used;
+  }
+  return L;
+}
+
+// adds the kernel durations of the step just launched (waits for it)
+int step_timing(FDPlan* p) {
+  if (!p->profile || p->marks_used == 0) return AMX_OK;
+  if (cudaEventSynchronize(p->marks[p->marks_used - 1]) != cudaSuccess) return AMX_ERR_CUDA;
+  cudaEvent_t prev = p->ev_start;
+  for (int i = 0; i < p->marks_used; ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, prev, p->marks[i]) != cudaSuccess) return AMX_ERR_CUDA;
+    p->prof_ms[p->marks_kind[i]] += ms;
+    p->prof_launches[p->marks_kind[i]] += 1;
+    prev = p->marks[i];
+  }
+  p->marks_used = 0;
+  return AMX_OK;
 }
 
 }  // namespace
@@ -160,6 +197,7 @@ int fd_plan_create(const amx_config& cfg, int64_t max_history, FDPlan** out) {
 
 void fd_plan_destroy(FDPlan* p) {
   if (!p) return;
+  fd_profile(p, 0);
   if (p->force) forcing_plan_destroy(p->force);
   if (p->wind_src) cudaFree(p->wind_src);
   if (p->ws) cudaFree(p->ws);
@@ -181,7 +219,7 @@ int fd_cfl_dt(FDPlan* p, const void* state, const amx_params& prm, double* dt_ho
   a.exact_end_time = 0;
   a.fixed_timestep = 0;
   a.t_end = INFINITY;
-  int rc = cfl(p, state, a, s);
+  int rc = cfl(p, p->L, state, a, s);
   rc |= ok(cudaMemcpyAsync(dt_host, &p->L.ctl->dt, sizeof(double), cudaMemcpyDeviceToHost, s));
   rc |= ok(cudaStreamSynchronize(s));
   return rc;
@@ -196,7 +234,7 @@ int fd_evolve(FDPlan* p, void* state, const amx_params& prm, double dt, cudaStre
   fd::k_set_dt<<<1, 1, 0, s>>>(p->L.ctl, dt);
   rc = ok(cudaGetLastError());
   if (rc) return rc;
-  rc = stages(p, state, make_args(p, prm, INFINITY), s);
+  rc = stages(p, p->L, state, make_args(p, prm, INFINITY), s);
   if (rc) return rc;
   return ok(cudaMemcpyAsync(&p->L.ctl->t, &t_before, sizeof(double), cudaMemcpyHostToDevice, s)) |
          ok(cudaStreamSynchronize(s));
@@ -206,10 +244,15 @@ int fd_run(FDPlan* p, void* state, const amx_params& prm, int64_t max_steps, dou
   const fd::FDArgs a = make_args(p, prm, t_pause);
   const int64_t check_every = 4;
   for (int64_t st = 0; st < max_steps; ++st) {
-    int rc = cfl(p, state, a, s);
+    const fd::FDLaunch L = step_launch(p, s);
+    int rc = cfl(p, L, state, a, s);
     // turbulent forcing between the dt and the evolve (time_integration.py:700-711)
-    if (p->force) rc |= forcing_apply(p->force, state, &p->L.ctl->dt, &p->L.ctl->active, &p->L.ctl->steps, prm, s);
-    rc |= stages(p, state, a, s);
+    if (p->force) {
+      rc |= forcing_apply(p->force, state, &p->L.ctl->dt, &p->L.ctl->active, &p->L.ctl->steps, prm, s);
+      fd::fd_mark(L, fd::FD_PH_FORCING, s);
+    }
+    rc |= stages(p, L, state, a, s);
+    rc |= step_timing(p);
     if (rc) return rc;
     if ((st + 1) % check_every == 0 && st + 1 < max_steps) {
       fd::FDControl h;
@@ -236,6 +279,35 @@ int fd_info(FDPlan* p, amx_run_info* info, cudaStream_t s) {
 }
 
 int fd_history(FDPlan*, double*, int64_t, cudaStream_t) { return AMX_ERR_UNSUPPORTED; }
+
+int fd_profile(FDPlan* p, int enable) {
+  if (enable && !p->profile) {
+    if (cudaEventCreate(&p->ev_start) != cudaSuccess) return AMX_ERR_CUDA;
+    for (int i = 0; i < fd::kFDMaxMarks; ++i)
+      if (cudaEventCreate(&p->marks[i]) != cudaSuccess) return AMX_ERR_CUDA;
+    p->profile = true;
+  } else if (!enable && p->profile) {
+    cudaEventDestroy(p->ev_start);
+    for (int i = 0; i < fd::kFDMaxMarks; ++i) cudaEventDestroy(p->marks[i]);
+    p->ev_start = nullptr;
+    p->profile = false;
+  }
+  return AMX_OK;
+}
+
+int fd_profile_read(FDPlan* p, double* ms, int64_t* launches, int n, int reset) {
+  for (int i = 0; i < n && i < fd::FD_PH_COUNT; ++i) {
+    if (ms) ms[i] = p->prof_ms[i];
+    if (launches) launches[i] = p->prof_launches[i];
+  }
+  if (reset) {
+    for (int i = 0; i < fd::FD_PH_COUNT; ++i) {
+      p->prof_ms[i] = 0.0;
+      p->prof_launches[i] = 0;
+    }
+  }
+  return AMX_OK;
+}
 
 int fd_status(FDPlan* p, int32_t* status_host, int32_t clear, cudaStream_t s) {
   int rc = ok(cudaMemcpyAsync(status_host, &p->L.ctl->status, sizeof(int), cudaMemcpyDeviceToHost, s)) |

@@ -20,5 +20,7 @@ int fd_run(FDPlan* p, void* state, const amx_params& prm, int64_t max_steps, dou
 int fd_info(FDPlan* p, amx_run_info* info, cudaStream_t s);
 int fd_history(FDPlan* p, double* dt_host, int64_t n, cudaStream_t s);
 int fd_status(FDPlan* p, int32_t* status_host, int32_t clear, cudaStream_t s);
+int fd_profile(FDPlan* p, int enable);
+int fd_profile_read(FDPlan* p, double* ms, int64_t* launches, int n, int reset);
 
 }  // namespace amx

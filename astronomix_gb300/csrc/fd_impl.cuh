@@ -110,11 +110,11 @@ __global__ void __launch_bounds__(kThreads) k_cfl(Bufs<T> b) {
       active = 1;
     } else {
       dt = a.C_cfl * a.dx / (lx + ly + lz);
-      dt = fmin(dt, a.dt_max);
+      dt = nanmin(dt, a.dt_max);
       active = (t < a.t_end) ? 1 : 0;
     }
     if (!(t < a.t_pause)) active = 0;
-    if (a.exact_end_time) dt = fmin(dt, a.t_end - t);
+    if (a.exact_end_time) dt = nanmin(dt, a.t_end - t);
     if (dt != dt) raise_status(&ctl->status, AMX_ERR_NAN);
     ctl->dt = dt;
     ctl->active = active;
@@ -189,23 +189,46 @@ __global__ void __launch_bounds__(kThreads) k_prep(Bufs<T> b, int stage) {
 
 // ---------------------------------------------------------------- WENO
 
-// Line tiles of A cells along the flux axis x 32 lanes across it; every
-// staged cell (A + 6 with the halo of 3) costs a flux and an eigensystem, so
-// longer tiles recompute less halo.  One block per SM leaves the shared
-// memory free: FP32 47 cells (212 KB; the 48 x 32 interfaces are six tasks
-// per thread; 256^3 step 0.097 s with 7 cells, 0.087 with 15, 0.084 with 31,
-// 0.082 with 47), FP64 15 cells (what fits in 227 KB).
-template <typename T> struct WenoTile {
-  static constexpr int A = sizeof(T) == 4 ? 47 : 15;  // cells per tile along the flux axis
-  static constexpr int L = 32;                        // lanes per tile across it
-  static constexpr int AH = A + 6;                    // staged cells along the axis (halo 3)
+// Staged per-cell values of a WENO tile, in the permuted frame (the flux
+// axis is "x"): the conserved state, the x-flux without its Bx row (always
+// zero), the inputs of the interface eigenvector blocks and the wave speeds.
+enum : int {
+  SV_U = 0,    // rho mx my mz E Bx By Bz
+  SV_F = 8,    // F: rho mx my mz E By Bz (F[Bx] = 0)
+  SV_EV = 15,  // floored rho, vx vy vz (unfloored rho), specific enthalpy
+  SV_C = 20,   // fast, Alfven, slow speed
+  kSV = 23
 };
-constexpr int kCellVals = 24;     // U(8) F(8) rho' vx vy vz h (5) cf ca cs (3)
+
+// Tile of A cells along the flux axis x 32 lanes across it.  Every staged
+// cell (A + 6 with the halo of 3) costs a flux and an eigensystem; every
+// thread owns whole interfaces.  Shared memory is a structure of arrays
+// with a row pitch of 33 values, so that a warp reading 32 lanes of one row
+// (the interface sweep) and a warp reading 32 cells of one lane (the
+// staging and the store of the z-axis tile) are both free of bank
+// conflicts.  FP32: A = 47, 384 threads (the 48 x 32 interfaces are four per
+// thread; 168 registers a thread, 12 warps per SM; the largest tile that
+// fits, 212 KB).  Measured on the 256^3 blast, s/step: 0.0499 (47, 384),
+// 0.0504 (32, 384), 0.0511 (32, 352), 0.0577 (31, 256: 255 registers,
+// 8 warps).  FP64: A = 15, 256 threads.
+#ifndef AMX_WENO_A32
+#define AMX_WENO_A32 47
+#endif
+#ifndef AMX_WENO_T32
+#define AMX_WENO_T32 384
+#endif
+template <typename T> struct WenoTile {
+  static constexpr int A = sizeof(T) == 4 ? AMX_WENO_A32 : 15;
+  static constexpr int THREADS = sizeof(T) == 4 ? AMX_WENO_T32 : 256;
+  static constexpr int L = 32;
+  static constexpr int LP = 33;
+  static constexpr int AH = A + 6;
+};
 
 template <typename T>
 constexpr size_t weno_smem() {
-  return sizeof(T) * ((size_t)WenoTile<T>::AH * WenoTile<T>::L * kCellVals +
-                      (size_t)(WenoTile<T>::A + 1) * WenoTile<T>::L * 8);
+  using W = WenoTile<T>;
+  return sizeof(T) * ((size_t)kSV * W::AH * W::LP + (size_t)7 * (W::A + 1) * W::LP);
 }
 
 __device__ __forceinline__ int pmod(int g, int n) {
@@ -213,17 +236,262 @@ __device__ __forceinline__ int pmod(int g, int n) {
   return r < 0 ? r + n : r;
 }
 
-// Interface fluxes along axis D (0 = x, 1 = y, 2 = z), _weno.py:112-324.
-// One block per SM: the characteristic projection needs about 250 registers
-// per thread; held to 128 (two blocks) it spilled 440 bytes per thread and
-// ran 18 % slower on the 256^3 blast.
+// index of a permuted-frame conserved row in the 7-vectors (Bx dropped):
+// rho mx my mz E By Bz -> 0..6, Bx -> -1
+__host__ __device__ constexpr int c7(int row) { return row < BX ? row : (row == BX ? -1 : row - 1); }
+
+// Everything a staged cell needs, with the arithmetic of _mhd_flux_x
+// (_fluxes.py:23-69 via primitive_state_from_conserved), of the per-cell
+// part of _eigenvector_building_blocks (_eigen.py:124-162) and of
+// _eigenvalue_building_blocks (_eigen.py:28-114), sharing the velocities.
+template <typename T>
+__device__ __forceinline__ void weno_cell(const T* U, T gamma, T rhomin, T pgmin, bool floors, T* out) {
+  const T rho = U[RHO];
+  const T vx = U[MX] / rho, vy = U[MY] / rho, vz = U[MZ] / rho;
+  const T Bx = U[BX], By = U[BY], Bz = U[BZ];
+  const T v2 = vx * vx + vy * vy + vz * vz;
+  const T b2 = Bx * Bx + By * By + Bz * Bz;
+  // flux (primitive_state_from_conserved_mhd, optional floors)
+  {
+    T p = (gamma - T(1)) * (U[EN] - T(0.5) * rho * v2 - T(0.5) * b2);
+    T rf = rho;
+    if (floors) {
+      rf = jmax(rho, rhomin);
+      p = jmax(p, pgmin);
+    }
+    const T ptot = p + T(0.5) * b2;
+    const T vdotB = vx * Bx + vy * By + vz * Bz;
+    const T E = p / (gamma - T(1)) + T(0.5) * rf * v2 + T(0.5) * b2;
+    out[SV_F + 0] = rf * vx;
+    out[SV_F + 1] = rf * (vx * vx) + ptot - Bx * Bx;
+    out[SV_F + 2] = rf * vx * vy - Bx * By;
+    out[SV_F + 3] = rf * vx * vz - Bx * Bz;
+    out[SV_F + 4] = (E + ptot) * vx - vdotB * Bx;
+    out[SV_F + 5] = By * vx - Bx * vy;
+    out[SV_F + 6] = Bz * vx - Bx * vz;
+  }
+  // eigen building blocks (floors always, _eigen.py:61-74 and :140-150)
+  // (each jnp.where re-tests its condition on the values already floored)
+  T pg = (gamma - T(1)) * (U[EN] - T(0.5) * (rho * v2 + b2));
+  const T r = ((rho < rhomin) || (pg < pgmin)) ? jmax(rho, rhomin) : rho;
+  pg = ((r < rhomin) || (pg < pgmin)) ? jmax(pg, pgmin) : pg;
+  const T energy = ((r < rhomin) || (pg < pgmin)) ? pg / (gamma - T(1)) + T(0.5) * (r * v2 + b2) : U[EN];
+  out[SV_EV + 0] = r;
+  out[SV_EV + 1] = vx;
+  out[SV_EV + 2] = vy;
+  out[SV_EV + 3] = vz;
+  out[SV_EV + 4] = (energy + pg) / r;
+  const T cs2 = jmax(T(0), gamma * Num<T>::abs_(pg / r));
+  const T b2r = b2 / r;
+  const T disc = dss(jmax(T(0), sq(b2r + cs2) - T(4) * (Bx * Bx) / r * cs2));
+  out[SV_C + 0] = dss(jmax(T(0), T(0.5) * (b2r + cs2 + disc)));
+  out[SV_C + 1] = dss(jmax(T(0), (Bx * Bx) / r));
+  out[SV_C + 2] = dss(jmax(T(0), T(0.5) * (b2r + cs2 - disc)));
+#pragma unroll
+  for (int k = 0; k < 8; ++k) out[SV_U + k] = U[k];
+}
+
+// Left eigenvector row S (_eigen.py:677-909) in the 7-vector layout, times
+// the 1/2 of the WENO inputs (_weno.py:185-188): an exact power-of-two
+// scaling, so the projections equal the reference's halved.
+template <typename T, int S>
+__device__ __forceinline__ void L7(const EigIF<T>& e, T* L) {
+  const T vx = e.vx, vy = e.vy, vz = e.vz, vsq = e.vsq, bty = e.bty, btz = e.btz, sbx = e.sbx;
+  const T a = e.a, cf = e.cf, cs = e.cs, af = e.af, aS = e.as, sr = e.sr;
+  const T gam0 = e.gam0, gam1 = e.gam1;
+  if constexpr (S == 0 || S == 6) {
+    // 0.5 L a2inv (x sbt when a < ca), halved: exact scalings of one product
+    const T q = (e.ge ? T(0.25) : T(0.25) * e.sbt) * e.a2inv;
+    if constexpr (S == 0) {
+      L[0] = af * (gam1 * vsq + cf * vx) - aS * cs * (bty * vy + btz * vz) * sbx;
+      L[1] = af * (gam0 * vx - cf);
+      L[2] = gam0 * af * vy + aS * cs * bty * sbx;
+      L[3] = gam0 * af * vz + aS * cs * btz * sbx;
+    } else {
+      L[0] = af * (gam1 * vsq - cf * vx) + aS * cs * (bty * vy + btz * vz) * sbx;
+      L[1] = af * (gam0 * vx + cf);
+      L[2] = gam0 * af * vy - aS * cs * bty * sbx;
+      L[3] = gam0 * af * vz - aS * cs * btz * sbx;
+    }
+    L[4] = -gam0 * af;
+    L[5] = gam0 * af * e.by + a * aS * bty * sr;
+    L[6] = gam0 * af * e.bz + a * aS * btz * sr;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) L[k] = L[k] * q;
+  } else if constexpr (S == 2 || S == 4) {
+    const T q = (e.ge ? T(0.25) * e.sbt : T(0.25)) * e.a2inv;
+    if constexpr (S == 2) {
+      L[0] = aS * (gam1 * vsq + cs * vx) + af * cf * (bty * vy + btz * vz) * sbx;
+      L[1] = gam0 * aS * vx - aS * cs;
+      L[2] = gam0 * aS * vy - af * cf * bty * sbx;
+      L[3] = gam0 * aS * vz - af * cf * btz * sbx;
+    } else {
+      L[0] = aS * (gam1 * vsq - cs * vx) - af * cf * (bty * vy + btz * vz) * sbx;
+      L[1] = aS * (gam0 * vx + cs);
+      L[2] = gam0 * aS * vy + af * cf * bty * sbx;
+      L[3] = gam0 * aS * vz + af * cf * btz * sbx;
+    }
+    L[4] = -gam0 * aS;
+    L[5] = gam0 * aS * e.by - a * af * bty * sr;
+    L[6] = gam0 * aS * e.bz - a * af * btz * sr;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) L[k] = L[k] * q;
+  } else if constexpr (S == 1 || S == 5) {
+    L[0] = T(0.25) * (btz * vy - bty * vz);
+    L[1] = T(0);
+    L[2] = T(0.25) * (-btz);
+    L[3] = T(0.25) * bty;
+    L[4] = T(0);
+    if constexpr (S == 1) {
+      L[5] = T(0.25) * (-btz * sbx * sr);
+      L[6] = T(0.25) * (bty * sbx * sr);
+    } else {
+      L[5] = T(0.25) * (btz * sbx * sr);
+      L[6] = T(0.25) * (-bty * sbx * sr);
+    }
+  } else {  // 3: entropy, -gam0 L a2inv, halved
+    const T q = T(0.5) * e.a2inv;
+    L[0] = -gam0 * (-e.a2 / gam0 - T(0.5) * vsq) * q;
+    L[1] = -gam0 * vx * q;
+    L[2] = -gam0 * vy * q;
+    L[3] = -gam0 * vz * q;
+    L[4] = -gam0 * T(-1) * q;
+    L[5] = -gam0 * e.by * q;
+    L[6] = -gam0 * e.bz * q;
+  }
+}
+
+// Right eigenvector column S (_eigen.py:392-620) in the 7-vector layout.
+template <typename T, int S>
+__device__ __forceinline__ void R7(const EigIF<T>& e, T* R) {
+  const T vx = e.vx, vy = e.vy, vz = e.vz, vsq = e.vsq, bty = e.bty, btz = e.btz, sbx = e.sbx;
+  const T a = e.a, a2 = e.a2, cf = e.cf, cs = e.cs, af = e.af, aS = e.as, sr = e.sr, gam2 = e.gam2;
+  if constexpr (S == 0) {
+    R[0] = af;
+    R[1] = af * (vx - cf);
+    R[2] = af * vy + aS * cs * bty * sbx;
+    R[3] = af * vz + aS * cs * btz * sbx;
+    R[4] = af * (cf * cf - cf * vx + T(0.5) * vsq - gam2 * a2) + aS * cs * (bty * vy + btz * vz) * sbx;
+    R[5] = a * aS * bty / sr;
+    R[6] = a * aS * btz / sr;
+  } else if constexpr (S == 6) {
+    R[0] = af;
+    R[1] = af * (vx + cf);
+    R[2] = af * vy - aS * cs * bty * sbx;
+    R[3] = af * vz - aS * cs * btz * sbx;
+    R[4] = af * (cf * cf + cf * vx + T(0.5) * vsq - gam2 * a2) - aS * cs * (bty * vy + btz * vz) * sbx;
+    R[5] = a * aS * bty / sr;
+    R[6] = a * aS * btz / sr;
+  } else if constexpr (S == 2) {
+    R[0] = aS;
+    R[1] = aS * (vx - cs);
+    R[2] = aS * vy - af * cf * bty * sbx;
+    R[3] = aS * vz - af * cf * btz * sbx;
+    R[4] = aS * (cs * cs - cs * vx + T(0.5) * vsq - gam2 * a2) - af * cf * (bty * vy + btz * vz) * sbx;
+    R[5] = -a * af * bty / sr;
+    R[6] = -a * af * btz / sr;
+  } else if constexpr (S == 4) {
+    R[0] = aS;
+    R[1] = aS * (vx + cs);
+    R[2] = aS * vy + af * cf * bty * sbx;
+    R[3] = aS * vz + af * cf * btz * sbx;
+    R[4] = aS * (cs * cs + cs * vx + T(0.5) * vsq - gam2 * a2) + af * cf * (bty * vy + btz * vz) * sbx;
+    R[5] = -a * af * bty / sr;
+    R[6] = -a * af * btz / sr;
+  } else if constexpr (S == 1 || S == 5) {
+    R[0] = T(0);
+    R[1] = T(0);
+    R[2] = -btz;
+    R[3] = bty;
+    R[4] = bty * vz - btz * vy;
+    if constexpr (S == 1) {
+      R[5] = -btz * sbx / sr;
+      R[6] = bty * sbx / sr;
+    } else {
+      R[5] = btz * sbx / sr;
+      R[6] = -bty * sbx / sr;
+    }
+  } else {  // 3
+    R[0] = T(1);
+    R[1] = vx;
+    R[2] = vy;
+    R[3] = vz;
+    R[4] = T(0.5) * vsq;
+    R[5] = T(0);
+    R[6] = T(0);
+  }
+  // fast modes flip when a < ca, slow modes when a >= ca
+  if constexpr (S == 0 || S == 6 || S == 2 || S == 4) {
+    const bool flip = (S == 0 || S == 6) ? !e.ge : e.ge;
+    if (flip) {
+#pragma unroll
+      for (int k = 0; k < 7; ++k) R[k] = R[k] * e.sbt;
+    }
+  }
+}
+
+// Nonzero entries of the rows and columns: the Alfven rows have no mx and E
+// entries, the Alfven columns no rho and mx, the entropy column no B.
+template <int S> __host__ __device__ constexpr unsigned lmask() { return (S == 1 || S == 5) ? 0x6Du : 0x7Fu; }
+template <int S> __host__ __device__ constexpr unsigned rmask() {
+  return (S == 1 || S == 5) ? 0x7Cu : (S == 3 ? 0x1Fu : 0x7Fu);
+}
+
+// One characteristic field of _weno.py:136-238 at one interface: project the
+// five flux and state differences of the stencil (dF[k] = F[i-1+k] -
+// F[i-2+k]), LF-split with alpha_s, WENO-weight both sides and add
+// R_s (third - second) to the interface flux.
+template <typename T, int S>
+__device__ __forceinline__ void weno_mode(const EigIF<T>& e, const T (&dF)[5][7], const T (&dq)[5][7], T alpha,
+                                          T (&Fi)[7]) {
+  constexpr unsigned LM = lmask<S>(), RM = rmask<S>();
+  T L[7];
+  L7<T, S>(e, L);
+  T d[5], q[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    T sd = T(0), sq_ = T(0);
+    bool first = true;
+#pragma unroll
+    for (int c = 0; c < 7; ++c) {
+      if (LM & (1u << c)) {
+        if (first) {
+          sd = L[c] * dF[k][c];
+          sq_ = L[c] * dq[k][c];
+          first = false;
+        } else {
+          sd = sd + L[c] * dF[k][c];
+          sq_ = sq_ + L[c] * dq[k][c];
+        }
+      }
+    }
+    d[k] = sd;
+    q[k] = sq_;
+  }
+  const T second = weno_phi(d[0] + alpha * q[0], d[1] + alpha * q[1], d[2] + alpha * q[2], d[3] + alpha * q[3]);
+  const T third = weno_phi(d[4] - alpha * q[4], d[3] - alpha * q[3], d[2] - alpha * q[2], d[1] - alpha * q[1]);
+  const T Fs = -second + third;
+  T R[7];
+  R7<T, S>(e, R);
+#pragma unroll
+  for (int c = 0; c < 7; ++c)
+    if (RM & (1u << c)) Fi[c] = Fi[c] + R[c] * Fs;
+}
+
+// Interface fluxes along axis D (0 = x, 1 = y, 2 = z), _weno.py:112-324,
+// with the flux difference into acc and the CT-corrected fluxes of the two
+// tangential field components (_constrained_transport.py:77-102) fused into
+// the store.
 template <typename T, int D>
-__global__ void __launch_bounds__(kThreads, 1) k_weno(Bufs<T> b) {
-  constexpr int kA = WenoTile<T>::A, kL = WenoTile<T>::L, kAH = WenoTile<T>::AH;
+__global__ void __launch_bounds__(WenoTile<T>::THREADS, 1) k_weno(Bufs<T> b) {
+  using W = WenoTile<T>;
+  constexpr int kA = W::A, kL = W::L, kLP = W::LP, kAH = W::AH, kT = W::THREADS;
   FD_ACTIVE_OR_RETURN(b.ctl);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* S = reinterpret_cast<T*>(smem_raw);          // [kAH][kL][kCellVals]
-  T* FI = S + (size_t)kAH * kL * kCellVals;      // [kA+1][kL][8] (permuted frame)
+  T* S = reinterpret_cast<T*>(smem_raw);        // [kSV][kAH][kLP]
+  T* FI = S + (size_t)kSV * kAH * kLP;          // [7][kA+1][kLP] (permuted frame)
+  auto sv = [&](int v, int ai, int li) -> T& { return S[((size_t)v * kAH + ai) * kLP + li]; };
+  auto fi = [&](int c, int ii, int li) -> T& { return FI[((size_t)c * (kA + 1) + ii) * kLP + li]; };
   const FDArgs a = b.a;
   const T gamma = T(a.gamma), rhomin = T(a.rhomin), pgmin = T(a.pgmin);
   const bool floors = a.enforce_positivity != 0;
@@ -242,8 +510,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_weno(Bufs<T> b) {
     return cidx(t3, gl, ga, n);
   };
 
-  // ---- stage the cells a0-3 .. a0+kA+2 (permuted frame)
-  for (int e = threadIdx.x; e < kAH * kL; e += blockDim.x) {
+  // ---- stage the cells a0-3 .. a0+kA+2 (permuted frame); the z tile walks
+  // along z within a warp so that its loads stay coalesced
+  for (int e = threadIdx.x; e < kAH * kL; e += kT) {
     int ai, li;
     if (D == 2) { ai = e % kAH; li = e / kAH; }
     else { li = e % kL; ai = e / kL; }
@@ -251,88 +520,82 @@ __global__ void __launch_bounds__(kThreads, 1) k_weno(Bufs<T> b) {
     int gl = l0 + li;
     if (gl >= n) gl = n - 1;
     const long long c = cell_of(ga, gl);
-    T* s = S + ((size_t)ai * kL + li) * kCellVals;
-    T U[8];
+    T U[8], out[kSV];
 #pragma unroll
     for (int r = 0; r < 8; ++r) U[r] = b.QC[perm_row(D, r) * nc + c];
-    T F[8], ev[5];
-    mhd_flux(U, F, gamma, rhomin, pgmin, floors);
-    eigvec_cell(U, gamma, rhomin, pgmin, ev);
-    T vx, cf, ca, cs;
-    eigenvalue_blocks(U, gamma, rhomin, pgmin, &vx, &cf, &ca, &cs);
+    weno_cell(U, gamma, rhomin, pgmin, floors, out);
 #pragma unroll
-    for (int r = 0; r < 8; ++r) { s[r] = U[r]; s[8 + r] = F[r]; }
-#pragma unroll
-    for (int r = 0; r < 5; ++r) s[16 + r] = ev[r];
-    s[21] = cf;
-    s[22] = ca;
-    s[23] = cs;
+    for (int v = 0; v < kSV; ++v) sv(v, ai, li) = out[v];
   }
   __syncthreads();
 
-  // ---- interfaces a0-1 .. a0+kA-1 (local ii = 0..kA): cell i = a0-1+ii is smem row ii+2
-  for (int task = threadIdx.x; task < (kA + 1) * kL; task += blockDim.x) {
-    const int li = task % kL, ii = task / kL;
-    const T* cst[6];
-#pragma unroll
-    for (int m = 0; m < 6; ++m) cst[m] = S + ((size_t)(ii + m) * kL + li) * kCellVals;
-    // eigenvector blocks from cells i (stencil 2) and i+1 (stencil 3)
-    EigIF<T> e;
-    eig_interface(cst[2] + 16, cst[3] + 16, cst[2][BX], cst[2][BY], cst[2][BZ], cst[3][BX], cst[3][BY], cst[3][BZ],
-                  gamma, e);
-    T Fint[8];
-#pragma unroll
-    for (int r = 0; r < 8; ++r)
-      Fint[r] = T(1.0 / 12.0) * (-cst[1][8 + r] + T(7) * cst[2][8 + r] + T(7) * cst[3][8 + r] - cst[4][8 + r]);
+  // ---- interfaces a0-1 .. a0+kA-1 (local ii = 0..kA): cell i = a0-1+ii is
+  // staged row ii+2, its stencil i-2 .. i+3 rows ii .. ii+5
 #pragma unroll 1
-    for (int s = 0; s < 7; ++s) {
-      T L[8];
-      L_row(e, s, L);
-      T sv[6], qv[6];
+  for (int task = threadIdx.x; task < (kA + 1) * kL; task += kT) {
+    const int li = task % kL, ii = task / kL;
+    // differences of the flux and the state over the stencil, and the base
+    // flux 1/12 (-F[i-1] + 7 F[i] + 7 F[i+1] - F[i+2])
+    T dF[5][7], dq[5][7], Fi[7];
+    {
+      T fp[7], qp[7], f1[7], f2[7], f3[7];
 #pragma unroll
       for (int m = 0; m < 6; ++m) {
-        T as = L[0] * cst[m][8], aq = L[0] * cst[m][0];
+        T f[7], q[7];
 #pragma unroll
-        for (int r = 1; r < 8; ++r) {
-          as = as + L[r] * cst[m][8 + r];
-          aq = aq + L[r] * cst[m][r];
+        for (int c = 0; c < 7; ++c) {
+          f[c] = sv(SV_F + c, ii + m, li);
+          q[c] = sv(SV_U + (c < 5 ? c : c + 1), ii + m, li);
         }
-        sv[m] = as;
-        qv[m] = aq;
-      }
-      T d[5], dq[5];
+        if (m > 0) {
 #pragma unroll
-      for (int k = 0; k < 5; ++k) { d[k] = sv[k + 1] - sv[k]; dq[k] = qv[k + 1] - qv[k]; }
-      // alpha_s: max |lambda_s| over the six stencil cells (cell centred)
-      T amx = T(0);
-#pragma unroll
-      for (int m = 0; m < 6; ++m) {
-        const T vx = cst[m][17], cf = cst[m][21], ca = cst[m][22], cs = cst[m][23];
-        T lam;
-        switch (s) {
-          case 0: lam = vx - cf; break;
-          case 1: lam = vx - ca; break;
-          case 2: lam = vx - cs; break;
-          case 3: lam = vx; break;
-          case 4: lam = vx + cs; break;
-          case 5: lam = vx + ca; break;
-          default: lam = vx + cf; break;
+          for (int c = 0; c < 7; ++c) {
+            dF[m - 1][c] = f[c] - fp[c];
+            dq[m - 1][c] = q[c] - qp[c];
+          }
         }
-        amx = (m == 0) ? Num<T>::abs_(lam) : jmax(amx, Num<T>::abs_(lam));
-      }
-      const T second = weno_phi(T(0.5) * (d[0] + amx * dq[0]), T(0.5) * (d[1] + amx * dq[1]),
-                                T(0.5) * (d[2] + amx * dq[2]), T(0.5) * (d[3] + amx * dq[3]));
-      const T third = weno_phi(T(0.5) * (d[4] - amx * dq[4]), T(0.5) * (d[3] - amx * dq[3]),
-                               T(0.5) * (d[2] - amx * dq[2]), T(0.5) * (d[1] - amx * dq[1]));
-      const T Fs = -second + third;
-      T R[8];
-      R_col(e, s, R);
 #pragma unroll
-      for (int r = 0; r < 8; ++r) Fint[r] = Fint[r] + R[r] * Fs;
+        for (int c = 0; c < 7; ++c) {
+          fp[c] = f[c];
+          qp[c] = q[c];
+          if (m == 1) f1[c] = f[c];
+          if (m == 2) f2[c] = f[c];
+          if (m == 3) f3[c] = f[c];
+          if (m == 4) Fi[c] = T(1.0 / 12.0) * (-f1[c] + T(7) * f2[c] + T(7) * f3[c] - f[c]);
+        }
+      }
     }
-    T* fo = FI + ((size_t)ii * kL + li) * 8;
+    // alpha_s = max |lambda_s| over the six stencil cells (cell centred)
+    T al[7];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) fo[r] = Fint[r];
+    for (int m = 0; m < 6; ++m) {
+      const T vx = sv(SV_EV + 1, ii + m, li), cf = sv(SV_C + 0, ii + m, li), ca = sv(SV_C + 1, ii + m, li),
+              cs = sv(SV_C + 2, ii + m, li);
+      const T lam[7] = {vx - cf, vx - ca, vx - cs, vx, vx + cs, vx + ca, vx + cf};
+#pragma unroll
+      for (int s = 0; s < 7; ++s) al[s] = (m == 0) ? Num<T>::abs_(lam[s]) : jmax(al[s], Num<T>::abs_(lam[s]));
+    }
+    // eigenvector blocks from cells i (row ii+2) and i+1 (row ii+3)
+    EigIF<T> e;
+    {
+      T cL[5], cR[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) {
+        cL[k] = sv(SV_EV + k, ii + 2, li);
+        cR[k] = sv(SV_EV + k, ii + 3, li);
+      }
+      eig_interface(cL, cR, sv(SV_U + BX, ii + 2, li), sv(SV_U + BY, ii + 2, li), sv(SV_U + BZ, ii + 2, li),
+                    sv(SV_U + BX, ii + 3, li), sv(SV_U + BY, ii + 3, li), sv(SV_U + BZ, ii + 3, li), gamma, e);
+    }
+    weno_mode<T, 0>(e, dF, dq, al[0], Fi);
+    weno_mode<T, 1>(e, dF, dq, al[1], Fi);
+    weno_mode<T, 2>(e, dF, dq, al[2], Fi);
+    weno_mode<T, 3>(e, dF, dq, al[3], Fi);
+    weno_mode<T, 4>(e, dF, dq, al[4], Fi);
+    weno_mode<T, 5>(e, dF, dq, al[5], Fi);
+    weno_mode<T, 6>(e, dF, dq, al[6], Fi);
+#pragma unroll
+    for (int c = 0; c < 7; ++c) fi(c, ii, li) = Fi[c];
   }
   __syncthreads();
 
@@ -340,33 +603,35 @@ __global__ void __launch_bounds__(kThreads, 1) k_weno(Bufs<T> b) {
   // lab rows of the two tangential B components whose fluxes CT corrects
   constexpr int T1 = (D == 0) ? BY : BX;
   constexpr int T2 = (D == 2) ? BY : BZ;
-  for (int task = threadIdx.x; task < kA * kL; task += blockDim.x) {
+  for (int task = threadIdx.x; task < kA * kL; task += kT) {
     int ci, li;
     if (D == 2) { ci = task % kA; li = task / kA; }
     else { li = task % kL; ci = task / kL; }
     const int ga = a0 + ci, gl = l0 + li;
     if (ga >= n || gl >= n) continue;
     const long long c = cell_of(ga, gl);
-    const T* fr = FI + ((size_t)(ci + 1) * kL + li) * 8;  // face i+1/2
-    const T* fl = FI + ((size_t)ci * kL + li) * 8;        // face i-1/2
+    // face i+1/2 is local interface ci+1, face i-1/2 is ci
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
-      const int pr = perm_row(D, r);
-      const T dF = fr[pr] - fl[pr];
+      const int k = c7(perm_row(D, r));
+      if (k < 0) {
+        if (D == 0) b.ACC[r * nc + c] = T(0);  // the x-flux of Bx vanishes
+        continue;
+      }
+      const T dF = fi(k, ci + 1, li) - fi(k, ci, li);
       if (D == 0) b.ACC[r * nc + c] = dF;
       else b.ACC[r * nc + c] = b.ACC[r * nc + c] + dF;
     }
-    // c2f over cells i-1 .. i+2 (smem rows ci+2 .. ci+5) of B_d and v_t (lab frame)
-    const T* sm = S + ((size_t)(ci + 2) * kL + li) * kCellVals;  // cell i-1
-    const T* s0 = sm + kL * kCellVals;                           // cell i
-    const T* s1 = s0 + kL * kCellVals;
-    const T* s2 = s1 + kL * kCellVals;
-    const T Bn = c2f(sm[BX], s0[BX], s1[BX], s2[BX]);  // permuted-frame x = lab axis D
-    const int m1 = perm_row(D, T1 - BX + MX), m2 = perm_row(D, T2 - BX + MX);
-    const T v1 = c2f(sm[m1] / sm[RHO], s0[m1] / s0[RHO], s1[m1] / s1[RHO], s2[m1] / s2[RHO]);
-    const T v2 = c2f(sm[m2] / sm[RHO], s0[m2] / s0[RHO], s1[m2] / s1[RHO], s2[m2] / s2[RHO]);
-    b.M[(2 * D) * nc + c] = fr[perm_row(D, T1)] + Bn * v1;
-    b.M[(2 * D + 1) * nc + c] = fr[perm_row(D, T2)] + Bn * v2;
+    // c2f over cells i-1 .. i+2 (staged rows ci+2 .. ci+5) of B_d and v_t (lab frame)
+    const T Bn = c2f(sv(SV_U + BX, ci + 2, li), sv(SV_U + BX, ci + 3, li), sv(SV_U + BX, ci + 4, li),
+                     sv(SV_U + BX, ci + 5, li));
+    constexpr int m1 = perm_row_c(D, T1 - BX + MX) - MX, m2 = perm_row_c(D, T2 - BX + MX) - MX;
+    const T v1 = c2f(sv(SV_EV + 1 + m1, ci + 2, li), sv(SV_EV + 1 + m1, ci + 3, li),
+                     sv(SV_EV + 1 + m1, ci + 4, li), sv(SV_EV + 1 + m1, ci + 5, li));
+    const T v2 = c2f(sv(SV_EV + 1 + m2, ci + 2, li), sv(SV_EV + 1 + m2, ci + 3, li),
+                     sv(SV_EV + 1 + m2, ci + 4, li), sv(SV_EV + 1 + m2, ci + 5, li));
+    b.M[(2 * D) * nc + c] = fi(c7(perm_row_c(D, T1)), ci + 1, li) + Bn * v1;
+    b.M[(2 * D + 1) * nc + c] = fi(c7(perm_row_c(D, T2)), ci + 1, li) + Bn * v2;
   }
 }
 
@@ -604,24 +869,33 @@ int launch_stages(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t 
   Bufs<T> b = make_bufs<T>(L, state, a);
   const int g = L.grid;
   const int n = L.n;
-  constexpr int kA = WenoTile<T>::A, kL = WenoTile<T>::L;
+  constexpr int kA = WenoTile<T>::A, kL = WenoTile<T>::L, kWT = WenoTile<T>::THREADS;
   const dim3 wg((n + kA - 1) / kA, (n + kL - 1) / kL, n);
   const size_t wsm = weno_smem<T>();
   for (int st = 0; st < 5; ++st) {
     k_prep<T><<<g, kThreads, 0, s>>>(b, st);
-    k_weno<T, 0><<<wg, kThreads, wsm, s>>>(b);
-    k_weno<T, 1><<<wg, kThreads, wsm, s>>>(b);
-    k_weno<T, 2><<<wg, kThreads, wsm, s>>>(b);
+    fd_mark(L, FD_PH_PREP, s);
+    k_weno<T, 0><<<wg, kWT, wsm, s>>>(b);
+    fd_mark(L, FD_PH_WENO_X, s);
+    k_weno<T, 1><<<wg, kWT, wsm, s>>>(b);
+    fd_mark(L, FD_PH_WENO_Y, s);
+    k_weno<T, 2><<<wg, kWT, wsm, s>>>(b);
+    fd_mark(L, FD_PH_WENO_Z, s);
     k_emf<T><<<g, kThreads, 0, s>>>(b);
+    fd_mark(L, FD_PH_EMF, s);
     k_emf_avg<T><<<g, kThreads, 0, s>>>(b);
+    fd_mark(L, FD_PH_EMF_AVG, s);
     if (a.wind) {
       const long long wn3 = (long long)a.wind_n * a.wind_n * a.wind_n;
       const int wg = (int)((wn3 + kThreads - 1) / kThreads < g ? (wn3 + kThreads - 1) / kThreads : g);
       k_wind_source<T><<<wg, kThreads, 0, s>>>(b, st);
+      fd_mark(L, FD_PH_WIND, s);
     }
     k_update<T><<<g, kThreads, 0, s>>>(b, st);
+    fd_mark(L, FD_PH_UPDATE, s);
   }
   k_finalize<T><<<g, kThreads, 0, s>>>(b);
+  fd_mark(L, FD_PH_FINALIZE, s);
   return cudaGetLastError() == cudaSuccess ? AMX_OK : AMX_ERR_CUDA;
 }
 
@@ -629,6 +903,7 @@ template <typename T>
 int launch_cfl(const FDLaunch& L, const void* state, const FDArgs& a, cudaStream_t s) {
   Bufs<T> b = make_bufs<T>(L, const_cast<void*>(state), a);
   k_cfl<T><<<L.grid, kThreads, 0, s>>>(b);
+  fd_mark(L, FD_PH_CFL, s);
   return cudaGetLastError() == cudaSuccess ? AMX_OK : AMX_ERR_CUDA;
 }
 

@@ -69,6 +69,13 @@ struct FDArgs {
   int wind_n;
 };
 
+// kernels of a step, for the per-kernel timing of amx_plan_profile
+enum FDPhase {
+  FD_PH_CFL = 0, FD_PH_PREP, FD_PH_WENO_X, FD_PH_WENO_Y, FD_PH_WENO_Z, FD_PH_EMF, FD_PH_EMF_AVG, FD_PH_WIND,
+  FD_PH_UPDATE, FD_PH_FINALIZE, FD_PH_FORCING, FD_PH_COUNT
+};
+constexpr int kFDMaxMarks = 48;  // launches of one step (37, 42 with the wind source) + 1
+
 // buffers and launch geometry handed from the host plan to the typed launchers
 struct FDLaunch {
   int grid;        // blocks of the pointwise sweeps
@@ -76,7 +83,20 @@ struct FDLaunch {
   void* bufs[10];  // Q0 Q QF QC ACC (8 rows) B BF (3) M (6) OM OB (3)
   FDControl* ctl;
   void* wind_src;  // stellar wind: [5][wind_n^3] source of the current stage (null without)
+  // per-kernel timing (null when off): an event is recorded after every
+  // launch, and marks_kind[i] names the kernel that ends at marks[i]
+  cudaEvent_t* marks;
+  int* marks_kind;
+  int* marks_used;
 };
+
+// records the end of a launch of kind `k` (no-op when timing is off)
+inline void fd_mark(const FDLaunch& L, int k, cudaStream_t s) {
+  if (!L.marks || *L.marks_used >= kFDMaxMarks) return;
+  L.marks_kind[*L.marks_used] = k;
+  cudaEventRecord(L.marks[*L.marks_used], s);
+  ++*L.marks_used;
+}
 
 int fd_set_attrs_f32();
 int fd_set_attrs_f64();
@@ -502,6 +522,13 @@ __device__ __forceinline__ int perm_row(int d, int row) {
     if (row == BZ) return BX;
   }
   return row;
+}
+
+// the same permutation, usable in constant expressions
+__host__ __device__ constexpr int perm_row_c(int d, int row) {
+  return d == 1   ? (row == MX ? MY : row == MY ? MX : row == BX ? BY : row == BY ? BX : row)
+         : d == 2 ? (row == MX ? MZ : row == MZ ? MX : row == BX ? BZ : row == BZ ? BX : row)
+                  : row;
 }
 
 }  // namespace fd

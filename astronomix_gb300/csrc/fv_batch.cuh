@@ -378,7 +378,7 @@ fv_batch_kernel(BatchArgs<T> b) {
 #pragma unroll
         for (int k = 0; k < DIM; ++k) sum = (k == 0) ? last_max(r, k) / dx : sum + last_max(r, k) / dx;
         double dt = b.base.C_cfl * 1.0 / sum;
-        if (b.base.exact_end_time) dt = fmin(dt, t_end - t);
+        if (b.base.exact_end_time) dt = nanmin(dt, t_end - t);
         if (dt > 0.0 && dt == dt) {
           s_dt[r] = dt;
           f |= 1;

@@ -94,6 +94,7 @@ struct FVArgs {
   int dt_dev;        // seam modes: dt from ctl->dt (times dt_scale), nothing done unless ctl->active
   double tol;        // fixed-point tolerance
   int max_iters;     // fixed-point cap (1000 in the reference)
+  unsigned long long spin_limit;  // polls before a grid barrier gives up (AMX_ERR_TIMEOUT)
   int mhd;           // the state carries B (the magnetic split is active)
   int split;         // 1: dimensionally split MUSCL-Hancock sweeps instead of SSP-RK2
   int first_order;   // split: piecewise-constant interface states
@@ -1145,7 +1146,7 @@ fv_run_kernel(FVArgs<T> a) {
   __shared__ double red[32];
   FVControl* ctl = a.ctl;
   int* status = &ctl->status;
-  const GridBarrier bar{&ctl->bar_count, &ctl->abort_flag};
+  const GridBarrier bar{&ctl->bar_count, &ctl->abort_flag, a.spin_limit};
   const long long nc = a.ncells;
   T* gas = a.state;
   constexpr int NVG_ = DIM + 2;
@@ -1300,7 +1301,7 @@ fv_run_kernel(FVArgs<T> a) {
 #pragma unroll
       for (int k = 1; k < DIM; ++k) w = nanmax(w, m[k]);
       double dt = a.C_cfl * a.dx / w;
-      if (a.use_dt_max && dt == dt) dt = fmin(dt, a.dt_max);
+      if (a.use_dt_max) dt = nanmin(dt, a.dt_max);
       return dt;
     }
     double sum = 0.0;
@@ -1336,8 +1337,9 @@ fv_run_kernel(FVArgs<T> a) {
     }
     if (!cfl_phase()) return;
     double dt = a.fixed_timestep ? a.dt_fixed : dt_from_maxima();
-    if (a.exact_end_time) dt = fmin(dt, a.t_end - t);
+    if (a.exact_end_time) dt = nanmin(dt, a.t_end - t);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (dt != dt) raise_status(status, AMX_ERR_NAN);
       ctl->dt = dt;
       ctl->active = 1;
     }
@@ -1445,7 +1447,9 @@ fv_run_kernel(FVArgs<T> a) {
       if (!(t < a.t_end)) break;
       dt = dt_from_maxima();
     }
-    if (a.exact_end_time) dt = fmin(dt, a.t_end - t);
+    if (a.exact_end_time) dt = nanmin(dt, a.t_end - t);
+    // a NaN dt is taken, as the reference takes it (its time then stops the loop)
+    if (dt != dt && blockIdx.x == 0 && threadIdx.x == 0) raise_status(status, AMX_ERR_NAN);
     const T dtT = T(dt);
     int it = 0;
     const long long idx = step0 + s;

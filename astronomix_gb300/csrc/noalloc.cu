@@ -23,7 +23,10 @@
 //    overlap on the GPU (two streams, or two host threads) race on it;
 //  * the first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture begins.
+//    before any stream capture begins;
+//  * with a non-null `info` the call reads the control block back and
+//    synchronises the stream; a capturing stream may not be synchronised, so
+//    such a call on one returns AMX_ERR_INVALID_ARG before launching anything.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -32,6 +35,7 @@
 #include "../../include/amx.h"
 #include "fv_kernels.cuh"
 #include "fv_registry.h"
+#include "validate.h"
 
 namespace {
 
@@ -61,30 +65,25 @@ int scratch_address(unsigned char** out) {
   return AMX_OK;
 }
 
+// The plan's validation plus what needs no allocation: FV only, and none of
+// the cuFFT-based physics that run between the kernel's phases.
 int check_config(const amx_config* c) {
-  if (!c) return AMX_ERR_INVALID_ARG;
+  const int rc = amx::validate_config(c);
+  if (rc) return rc;
   if (c->solver_mode != AMX_FINITE_VOLUME) return AMX_ERR_UNSUPPORTED;
-  // need cuFFT work between the phases of a step
   if (c->self_gravity || c->turbulent_forcing || c->stellar_wind) return AMX_ERR_UNSUPPORTED;
-  if (c->dtype != AMX_F32 && c->dtype != AMX_F64) return AMX_ERR_INVALID_ARG;
-  if (c->dimensionality < 1 || c->dimensionality > 3 || c->num_cells < 4) return AMX_ERR_INVALID_ARG;
-  if (c->num_vars != c->dimensionality + 2 + (c->mhd ? 3 : 0)) return AMX_ERR_INVALID_ARG;
-  if (c->mhd && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
-  if (c->split != 0 && c->split != 1) return AMX_ERR_INVALID_ARG;
-  if (c->riemann_solver < AMX_HLL || c->riemann_solver > AMX_LAX_FRIEDRICHS) return AMX_ERR_UNSUPPORTED;
-  if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA) return AMX_ERR_UNSUPPORTED;
-  if (!(c->grid_spacing > 0.0)) return AMX_ERR_INVALID_ARG;
-  if (c->boundary_handling == AMX_GHOST_CELLS) {
-    for (int k = 0; k < c->dimensionality; ++k) {
-      for (int side = 0; side < 2; ++side) {
-        const int b = side ? c->bc_hi[k] : c->bc_lo[k];
-        if (b != AMX_BC_OPEN && b != AMX_BC_PERIODIC && b != AMX_BC_REFLECTIVE) return AMX_ERR_UNSUPPORTED;
-        if (c->mhd && b == AMX_BC_REFLECTIVE) return AMX_ERR_UNSUPPORTED;
-      }
-      if ((c->bc_lo[k] == AMX_BC_PERIODIC) != (c->bc_hi[k] == AMX_BC_PERIODIC)) return AMX_ERR_UNSUPPORTED;
-    }
-  }
   return AMX_OK;
+}
+
+// Cells of the grid, or -1 when they exceed `limit` (checked after every
+// factor, so that no product can overflow).
+long long cells_within(const amx_config* c, long long limit) {
+  long long nc = 1;
+  for (int k = 0; k < c->dimensionality; ++k) {
+    nc *= c->num_cells;
+    if (nc > limit) return -1;
+  }
+  return nc;
 }
 
 template <typename T>
@@ -127,6 +126,7 @@ int launch(const amx_config* c, void* state, const amx_params* prm, int64_t max_
   a.dt_max = prm->dt_max;
   a.p2 = a.mag0;
   a.max_iters = 1000;
+  a.spin_limit = AMX_BARRIER_SPIN_LIMIT;
   a.t_pause = INFINITY;
   const int64_t chunk = int64_t(1) << 16;
   for (int64_t done = 0; done < max_steps; done += chunk) {
@@ -148,9 +148,17 @@ extern "C" int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_
   int rc = check_config(cfg);
   if (rc) return rc;
   if (!state || !prm || max_steps < 0) return AMX_ERR_INVALID_ARG;
-  long long nc = 1;
-  for (int k = 0; k < cfg->dimensionality; ++k) nc *= cfg->num_cells;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (info) {
+    // reading the status back synchronises the stream, which a capture forbids
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return AMX_ERR_CUDA;
+    if (cs != cudaStreamCaptureStatusNone) return AMX_ERR_INVALID_ARG;
+  }
   const size_t elem = cfg->dtype == AMX_F32 ? 4 : 8;
+  // no grid with more values than the scratch holds can fit: refuse it before any product could overflow
+  const long long nc = cells_within(cfg, (long long)(kNoallocScratchBytes / elem));
+  if (nc < 0) return AMX_ERR_TOO_LARGE;
   const size_t field = (size_t)nc * elem;
   const size_t o_p1 = align256(sizeof(amx::FVControl));
   const size_t o_m0 = align256(o_p1 + (cfg->dimensionality + 2) * field);
@@ -164,10 +172,12 @@ extern "C" int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_
 
   amx::FVKernelInfo kinfo{};
   const int rs = (cfg->riemann_solver == AMX_HLLC_LM) ? AMX_HLLC : cfg->riemann_solver;
-  const int scheme = cfg->split ? amx::FV_SPLIT : amx::FV_UNSPLIT;
+  const int scheme = cfg->split ? amx::FV_SPLIT
+                                 : (cfg->limiter == AMX_VAN_ALBADA_PP ? amx::FV_UNSPLIT_PP : amx::FV_UNSPLIT);
   const bool ok = (cfg->dtype == AMX_F32) ? amx::fv_kernel_f32(cfg->dimensionality, rs, cfg->mhd != 0, scheme, &kinfo)
                                           : amx::fv_kernel_f64(cfg->dimensionality, rs, cfg->mhd != 0, scheme, &kinfo);
   if (!ok) return AMX_ERR_UNSUPPORTED;
+  if (scheme == amx::FV_UNSPLIT_PP) kinfo.smem += kinfo.smem_pp;  // as amx_plan_create
   if (cudaFuncSetAttribute(kinfo.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kinfo.smem) != cudaSuccess)
     return AMX_ERR_CUDA;
   int dev = 0, sms = 0, per_sm = 0;
@@ -180,7 +190,6 @@ extern "C" int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_
   const long long want = (nc + amx::kFVThreads - 1) / amx::kFVThreads;
   const int grid = (int)(want < cap ? (want < 1 ? 1 : want) : cap);
 
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   // a fresh run: time, counters and status start at zero
   if (cudaMemsetAsync(scratch, 0, sizeof(amx::FVControl), s) != cudaSuccess) return AMX_ERR_CUDA;
   rc = (cfg->dtype == AMX_F32) ? launch<float>(cfg, state, prm, max_steps, scratch, o_p1, o_m0, o_m1, kinfo, grid, s)

@@ -1,19 +1,25 @@
-"""Benchmark: zone-updates/s of the FV MHD step on the 2D Orszag-Tang vortex, 512^2, FP32.
+"""Benchmark: zone-updates/s of the FD WENO-CT MHD step on the 3D blast, 256^3, FP32.
 
-One "step" is one time step of astronomix's finite-volume MHD scheme (CFL dt,
-SSP-RK2 hydro half step, implicit-midpoint magnetic sub-step, hydro half step)
-over the whole 512^2 grid, launched through the C ABI.  The Orszag-Tang state
-is synthetic (its analytic initial condition, advanced by warm-up steps).
+One "step" is one time step of astronomix's finite-difference MHD scheme
+(CFL dt, five SSPRK(5,4) stages of WENO fluxes in x, y, z + constrained
+transport, positivity floors) over the whole 256^3 periodic grid, launched
+through the C ABI.  The blast is synthetic: rho = 1, v = 0, p = 10 inside
+r < 0.1 of the centre and 0.1 outside, B = (1, 1, 0)/sqrt 2 with face fields
+from initialize_interface_fields, gamma 5/3, C_cfl 1.5 (no dataset).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Timing: each timed step is bracketed by CUDA events on the launching stream
-and the L2 cache (129 MB; the state is 7.3 MB) is flushed between steps by
-writing a 512 MB buffer, outside the events.  The line also carries the
-end-to-end number through the C ABI with host buffers (H2D + step + D2H per
-step), the FP64 throughput of the same kernels, the FP32-vs-FP64 L1 density
-error at t = 0.05, the roofline of the kernel and the CPU baseline (the
-oracle, a NumPy restatement of the reference, timed on this host).
+Timing: each timed step is bracketed by CUDA events on the launching stream;
+the state (738 MB) and the step's workspace (3.4 GB) are far larger than the
+L2 cache (129 MB), so no flush is needed between steps.  The line also
+carries: the end-to-end number through the C ABI with pinned host buffers
+(H2D + step + D2H per step); the per-kernel launch durations (CUDA events
+after every launch) and the roofline of the dominant kernel, k_weno; the
+FP64 throughput of the same kernels and the FP32-vs-FP64 relative L1
+density error of a full run to t_end = 0.02; the CPU baseline (the oracle,
+a NumPy restatement of the reference, on a bounded sample); and the
+secondary workloads (Orszag-Tang 512^2 FV, the reference's published blast
+workloads, the batched ensemble, the adjoint, self-gravity).
 
 With N > 1 (torchrun), every rank runs an independent replica of the
 workload (the step does not shard); value = sum of zone-updates / max time.
@@ -34,16 +40,26 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
-N_CELLS = 512
+N_CELLS = 256
 METRIC = "zone-updates/s on 1 GB300, FP32 fused vs plain FP64, at L1 err <=1e-5 vs FP64"
-WORKLOAD = "Orszag-Tang 2D MHD, FV HLL + Pang-Wu split (constrained B), MINMOD, SSP-RK2, 512x512 periodic, gamma 5/3"
+WORKLOAD = ("3D MHD blast, FD 5th-order WENO + constrained transport, SSPRK(5,4), 256^3 periodic unit cube, "
+            "gamma 5/3, rho 1, p 10 (r < 0.1) / 0.1, B (1,1,0)/sqrt2, C_cfl 1.5")
+OT_WORKLOAD = "Orszag-Tang 2D MHD, FV HLL + Pang-Wu split (constrained B), MINMOD, SSP-RK2, 512x512 periodic, gamma 5/3"
+
+
+def workload_config(n):
+    """The `config` of the JSON line, identical in both arms."""
+    return {"workload": WORKLOAD.replace("256^3", "%d^3" % n), "grid": [n, n, n],
+            "precision": "fp32 fields, fp64 dt/time/conservation sums",
+            "l2": "not flushed: state 738 MB + workspace 3.4 GB per step, far above the 129 MB L2" if n >= 128
+            else "state below the L2 size"}
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_CELLS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -51,15 +67,18 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-run batched ensemble")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the 128^3 adjoint workload")
     ap.add_argument("--no-gravity", action="store_true", help="skip the self-gravity collapse workload")
-    ap.add_argument("--case", default=None, choices=["fd", "fdsrc", "fv3d", "fvsplit", "ensemble", "adjoint",
-                                                     "gravity"],
+    ap.add_argument("--no-l1", action="store_true", help="skip the full FP32 and FP64 runs to t_end (L1 error)")
+    ap.add_argument("--no-ot", action="store_true", help="skip the Orszag-Tang 512^2 FV workload")
+    ap.add_argument("--case", default=None, choices=["fdblast", "fd", "fdsrc", "fv3d", "fvsplit", "ensemble",
+                                                     "adjoint", "gravity"],
                     help="run one small case of a secondary workload and exit (for profilers)")
     return ap.parse_args()
 
 
-def run_case(name):
-    """Small, self-contained runs of the secondary workloads for ncu captures:
-    fd: FD WENO-CT blast 128^3 FP32, 2 steps; fv3d: FV Lax-Friedrichs MHD
+def run_case(name, n=None):
+    """Small, self-contained runs of the workloads for ncu captures:
+    fdblast: the headline FD blast at --n^3 FP32, 2 steps (one warm-up);
+    fd: the reference's FD WENO-CT arena blast 128^3 FP32, 2 steps; fv3d: FV Lax-Friedrichs MHD
     blast 192^3 FP32, 2 steps (one launch); fvsplit: the same blast with the
     split MUSCL-Hancock scheme and HLLC; ensemble: 8 turbulent 2D MHD
     runs (128^2..512^2, t_end / 8) in one batched launch; adjoint: the 3D
@@ -71,7 +90,18 @@ def run_case(name):
     import torch
     from astronomix_gb300 import _native
 
-    if name in ("fd", "fv3d", "fvsplit"):
+    if name == "fdblast":
+        from _cases import blast_fd
+        from astronomix_gb300.time_integration import get_plan
+
+        cfg, prm, rv, s = blast_fd(n=n, dtype=np.float32, t_end=1e9)
+        plan = get_plan(cfg, rv, s.shape, np.float32)
+        dev = torch.from_numpy(s.astype(np.float32)).cuda()
+        st = torch.cuda.current_stream().cuda_stream
+        plan.reset(st)
+        info = plan.run(dev.data_ptr(), _native.make_params(prm), 2, st)
+        print(json.dumps({"case": name, "n": n, "steps": info.steps, "status": info.status}))
+    elif name in ("fd", "fv3d", "fvsplit"):
         from astronomix_gb300.time_integration import get_plan
 
         cfg, prm, rv, s = arena_blast(128 if name == "fd" else 192, "fv_split" if name == "fvsplit" else name[:2])
@@ -331,48 +361,6 @@ def time_fd_sources(n=256, steps=3):
     del dev
     return {"workload": "FD WENO-CT blast %d^3 + turbulent forcing + stellar-wind EI source" % n,
             "s_per_step": sps, "zone_updates_per_s": n ** 3 / sps, "finite": ok, "steps_timed": steps}
-
-
-def fd_precision(n=128, t_end=0.02, flop_per_zu=44e3):
-    """FD WENO-CT on the MHD blast of the FD workload (periodic unit cube,
-    rho = 1, p = 10 inside r < 0.1 and 0.1 outside, B = (1, 1, 0)/sqrt 2,
-    C_cfl 1.5, SSPRK(5,4)) at n^3 to t_end in FP32 and FP64 with the same
-    kernels: s/step of each, their ratio, and the relative L1 density error
-    of FP32 against FP64.  The FD kernel's compute roof is the measured FP32
-    FMA rate; `flop_per_zu` is the estimated arithmetic per zone-update of
-    the scheme (eigensystem once per interface, 7 characteristic fields)."""
-    import torch
-    from _cases import blast_fd
-    from astronomix_gb300 import _native
-    from astronomix_gb300.time_integration import get_plan
-
-    st = torch.cuda.current_stream()
-    out = {"grid": [n, n, n], "t_end": t_end}
-    res = {}
-    for name, dt in (("fp32", np.float32), ("fp64", np.float64)):
-        cfg, prm, rv, s = blast_fd(n=n, dtype=dt, t_end=t_end)
-        s = s.astype(dt)
-        plan = get_plan(cfg, rv, s.shape, dt)
-        p = _native.make_params(prm)
-        dev = torch.from_numpy(s).cuda()
-        plan.reset(st.cuda_stream)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(st)
-        info = plan.run(dev.data_ptr(), p, 1 << 40, st.cuda_stream)
-        b.record(st)
-        torch.cuda.synchronize()
-        res[name] = dev[0].double()
-        out[name] = {"steps": info.steps, "s_per_step": a.elapsed_time(b) / 1e3 / max(1, info.steps),
-                     "status": info.status}
-        del dev
-    out["fp32_over_fp64"] = out["fp64"]["s_per_step"] / out["fp32"]["s_per_step"]
-    out["l1_err_vs_fp64"] = float((res["fp32"] - res["fp64"]).abs().sum() / res["fp64"].abs().sum())
-    peak = _native.probe_fp32_fma(st.cuda_stream)
-    zu_s = n ** 3 / out["fp32"]["s_per_step"]
-    out["compute_roof"] = {"fp32_fma_tflops_measured": peak, "flop_per_zone_update_estimate": flop_per_zu,
-                           "achieved_tflops_estimate": zu_s * flop_per_zu / 1e12,
-                           "frac": zu_s * flop_per_zu / 1e12 / peak}
-    return out
 
 
 def time_ensemble(num_runs=64, sequential=True):
@@ -641,138 +629,76 @@ def load_traffic(name):
         return None
 
 
-def cpu_baseline_oracle(budget_s=15.0, n=128):
-    """The oracle (NumPy restatement of the reference) on a bounded sample: OT n^2, FP32."""
-    from _cases import orszag_tang
-    from oracle import driver
-
-    cfg, prm, rv, s = orszag_tang(n=n, t_end=10.0, dtype=np.float32)
-    P = s
-    steps = 0
-    t0 = time.perf_counter()
-    while time.perf_counter() - t0 < budget_s:
-        P = driver.time_integration(P, cfg, prm, rv, max_steps=1)
-        steps += 1
-    dt = time.perf_counter() - t0
-    return {"value": n * n * steps / dt, "unit": "zone-updates/s", "cores": 1, "kind": "port",
-            "sample": "oracle (NumPy restatement) OT %dx%d FP32, %d steps in %.1f s" % (n, n, steps, dt)}
-
-
-def _reference_replica(job):
-    """One host process of the reference arm: OT n^2 FP32 advanced by the
-    oracle one step at a time, `steps` steps or `budget` seconds."""
-    n, steps, budget = job
-    from _cases import orszag_tang
-    from oracle import driver
-
-    cfg, prm, rv, s = orszag_tang(n=n, t_end=10.0, dtype=np.float32)
-    P = driver.time_integration(s, cfg, prm, rv, max_steps=1)  # warm-up step
-    done = 0
-    t0 = time.perf_counter()
-    while done < steps:
-        P = driver.time_integration(P, cfg, prm, rv, max_steps=1)
-        done += 1
-        if time.perf_counter() - t0 > budget:
-            break
-    return done, time.perf_counter() - t0
+CPU_SAMPLE_N = 64
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the oracle port of the reference's CPU path on this
-    host, one independent replica per host core (processes started with
-    spawn, one NumPy thread each); value = the replicas' summed throughput."""
+    """--impl reference: the reference's algorithm on this host's cores.  The
+    reference is Python/JAX and JAX is not installed on these machines, so
+    this times the port of its FD step that the oracle keeps: the compiled
+    restatement oracle/cpu/fd_step.cpp (C++17, OpenMP over every host core),
+    which is bit-identical to the NumPy oracle and to the reference's own
+    results on the committed fixtures, on a bounded sample of the workload,
+    the same blast at 64^3; each of the --steps steps is one time step."""
     if rank != 0:
         return
-    import multiprocessing as mp
-
-    try:
-        cores = len(os.sched_getaffinity(0))
-    except AttributeError:
-        cores = os.cpu_count() or 1
-    budget = 60.0
-    os.environ.setdefault("OMP_NUM_THREADS", "1")
-    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_reference_replica, [(args.n, args.steps, budget)] * cores)
-    v = sum(args.n * args.n * d / t for d, t in res)
-    steps = min(d for d, _ in res)
-    ms = 1e3 * sum(t / d for d, t in res) / len(res)
+    m = CPU_SAMPLE_N
+    v, steps, dt, threads = cpu_fd_sample(m, budget_s=120.0, max_steps=max(1, args.steps))
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus,
-        "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "grid": [args.n, args.n], "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": cores, "kind": "port",
-                         "sample": "%d replicas x %d steps of OT %dx%d (each bounded to %.0f s)" % (
-                             cores, steps, args.n, args.n, budget)},
+        "config": workload_config(args.n),
+        "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": threads, "kind": "port",
+                         "sample": "compiled restatement of the reference's FD step, %d OpenMP threads, blast %d^3 "
+                                   "FP32, %d steps in %.1f s (after one warm-up step)" % (threads, m, steps, dt)},
         "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
 
-def run_ours(args, rank, world):
+def time_orszag_tang(n=512, K=100, t_cmp=0.5, flush_mb=512):
+    """The FV workload (Orszag-Tang 512^2, FP32): zone-updates/s with one
+    step per launch and the L2 flushed between steps (the state is 7.3 MB),
+    end to end through the C ABI with pinned host buffers, the FP64 rate of
+    the same kernels, the FP32-vs-FP64 relative L1 density error of full runs
+    to t_cmp, and the roofline of fv_run_kernel (HBM, algorithmic bytes)."""
     import torch
 
     from _cases import orszag_tang
     from astronomix_gb300 import _native
     from astronomix_gb300.time_integration import get_plan
 
-    dev_index = torch.cuda.current_device()
-    n = args.n
     cfg, prm, rv, s = orszag_tang(n=n, t_end=1e9, dtype=np.float32)
     p = _native.make_params(prm)
     plan = get_plan(cfg, rv, s.shape, np.float32)
     stream = torch.cuda.current_stream()
     st = stream.cuda_stream
     state = torch.from_numpy(s).cuda()
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    flush = torch.empty(flush_mb * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     plan.reset(st)
-
-    # warm-up: W steps, one launch each
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(5):
         plan.run_async(state.data_ptr(), p, 1, st)
     torch.cuda.synchronize()
     it0 = plan.run(state.data_ptr(), p, 0, st)
-
-    K = args.steps
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
-    barrier(world)
+    for i in range(K):
+        flush.zero_()
+        starts[i].record(stream)
+        plan.run_async(state.data_ptr(), p, 1, st)
+        ends[i].record(stream)
     torch.cuda.synchronize()
-    with ClockSampler(dev_index) as clk:
-        for i in range(K):
-            flush.zero_()
-            starts[i].record(stream)
-            plan.run_async(state.data_ptr(), p, 1, st)
-            ends[i].record(stream)
-        torch.cuda.synchronize()
-    barrier(world)
-    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    total_s = sum(step_ms) / 1e3
+    total_s = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / 1e3
     it1 = plan.run(state.data_ptr(), p, 0, st)
     k_mean = (it1.magnetic_iterations - it0.magnetic_iterations) / max(1, it1.steps - it0.steps)
-    status = it1.status
-    from astronomix_gb300.replicas import replica_throughput
-
-    value = replica_throughput(n * n * K, total_s)
-    total_s_max = max_over_ranks(total_s, world)
-
-    # ---- fused multi-step throughput (K steps in one launch, L2-resident state)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    plan.run_async(state.data_ptr(), p, K, st)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    fused_ms = e0.elapsed_time(e1)
-
-    # ---- end to end through the C ABI with host buffers (pinned)
+    value = n * n * K / total_s
+    # end to end through the C ABI with host buffers (pinned)
     host = torch.from_numpy(s.copy()).pin_memory()
     host_out = torch.empty_like(host).pin_memory()
     dev2 = torch.empty_like(state)
     nbytes = host.numel() * host.element_size()
-    Ke = max(10, min(K, 100))
+    Ke = 20
     es = [torch.cuda.Event(enable_timing=True) for _ in range(Ke)]
     ee = [torch.cuda.Event(enable_timing=True) for _ in range(Ke)]
     plan.reset(st)
@@ -784,64 +710,225 @@ def run_ours(args, rank, world):
         host_out.copy_(dev2, non_blocking=True)
         ee[i].record(stream)
     torch.cuda.synchronize()
-    e2e_s = sum(a.elapsed_time(b) for a, b in zip(es, ee)) / 1e3
-    e2e_value = replica_throughput(n * n * Ke, e2e_s)
-
-    # ---- FP64: same kernels, plain double precision
+    e2e = n * n * Ke / (sum(a.elapsed_time(b) for a, b in zip(es, ee)) / 1e3)
+    # FP64, same kernels
     cfg64, prm64, rv64, s64 = orszag_tang(n=n, t_end=1e9, dtype=np.float64)
     plan64 = get_plan(cfg64, rv64, s64.shape, np.float64)
     st64 = torch.from_numpy(s64).cuda()
     plan64.reset(st)
     for _ in range(3):
         plan64.run_async(st64.data_ptr(), p, 1, st)
-    K64 = max(5, K // 10)
-    t64 = []
-    for _ in range(K64):
-        flush.zero_()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        plan64.run_async(st64.data_ptr(), p, 1, st)
-        b.record(stream)
-        t64.append((a, b))
+    K64 = 10
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
-    fp64_s = sum(a.elapsed_time(b) for a, b in t64) / 1e3
-    fp64_value = n * n * K64 / fp64_s
-
-    # ---- accuracy: FP32 vs FP64 density at t = 0.05 from the same initial state
-    t_cmp = 0.05
-    cfgA, prmA, rvA, sA = orszag_tang(n=n, t_end=t_cmp, dtype=np.float32)
-    cfgB, prmB, rvB, sB = orszag_tang(n=n, t_end=t_cmp, dtype=np.float64)
-    a32 = torch.from_numpy(sA).cuda()
-    a64 = torch.from_numpy(sB).cuda()
-    pa, pb = _native.make_params(prmA), _native.make_params(prmB)
-    planA = get_plan(cfgA, rvA, sA.shape, np.float32)
-    planB = get_plan(cfgB, rvB, sB.shape, np.float64)
-    planA.reset(st)
-    planB.reset(st)
-    infoA = planA.run(a32.data_ptr(), pa, 1 << 40, st)
-    infoB = planB.run(a64.data_ptr(), pb, 1 << 40, st)
-    r32 = a32[0].double()
-    r64 = a64[0]
-    l1 = float((r32 - r64).abs().sum() / r64.abs().sum())
-
-    # ---- roofline of the dominant (only) kernel: fv_run_kernel
+    a.record(stream)
+    plan64.run_async(st64.data_ptr(), p, K64, st)
+    b.record(stream)
+    torch.cuda.synchronize()
+    fp64_value = n * n * K64 / (a.elapsed_time(b) / 1e3)
+    # FP32 vs FP64 at t_cmp from the same initial state
+    res = {}
+    steps = {}
+    for name, dt in (("fp32", np.float32), ("fp64", np.float64)):
+        c_, pr_, rv_, s_ = orszag_tang(n=n, t_end=t_cmp, dtype=dt)
+        pl = get_plan(c_, rv_, s_.shape, dt)
+        d_ = torch.from_numpy(s_.astype(dt)).cuda()
+        pl.reset(st)
+        info = pl.run(d_.data_ptr(), _native.make_params(pr_), 1 << 40, st)
+        res[name] = d_[0].double()
+        steps[name] = info.steps
+    l1 = float((res["fp32"] - res["fp64"]).abs().sum() / res["fp64"].abs().sum())
     bpz = algorithmic_bytes_per_zone_update(k_mean)
-    launch_s = total_s / K
-    achieved = bpz * n * n / launch_s / 1e9
-    peaks = {}
+    achieved = bpz * n * n / (total_s / K) / 1e9
+    peak, peak_src = hbm_peak()
+    return {"workload": OT_WORKLOAD, "value": value, "unit": "zone-updates/s", "ms_per_step": 1e3 * total_s / K,
+            "steps": K, "l2": "flushed between timed steps (%d MB write); state 7.3 MB" % flush_mb,
+            "e2e": {"value": e2e, "unit": "zone-updates/s", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes},
+            "fp64_value": fp64_value, "fp32_over_fp64": value / fp64_value,
+            "l1_err_vs_fp64": l1, "l1_t_end": t_cmp, "l1_steps": [steps["fp32"], steps["fp64"]],
+            "magnetic_iterations_mean": k_mean,
+            "roofline": {"bound": "hbm", "kernel": "fv_run_kernel", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": load_traffic("fv_run_kernel_ot512_fp32_step"),
+                         "note": "algorithmic %.0f B/zone-update (k = %.2f fixed-point iterations), peak %s" % (
+                             bpz, k_mean, peak_src)}}
+
+
+def hbm_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-        peak, peak_src = float(peaks["hbm_gbs"]), "measured"
+            return float(json.load(f)["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
-        peak, peak_src = 6800.0, "fallback"
-    traffic = load_traffic("fv_run_kernel_ot512_fp32_step")
+        return 6800.0, "fallback"
 
+
+# FD algorithmic figures (FP32).  A step reads and writes 11 words per cell per
+# array pass, 16 array passes: 704 B per zone-update.  One k_weno launch reads
+# the cell-centre state (8 words) and writes the flux difference (8) and two
+# CT-corrected fluxes (2); the y and z launches also read the flux difference
+# they accumulate into (8): 18 / 26 / 26 words per cell, 23.3 on average.
+FD_STEP_BYTES_PER_ZU = 704
+WENO_BYTES_PER_CELL = 4 * (18 + 26 + 26) / 3.0
+
+
+def cpu_fd_sample(n, budget_s, max_steps=1 << 30):
+    """The oracle's compiled restatement of the reference's FD step
+    (oracle/cpu/fd_step.cpp, bit-identical to the NumPy oracle and to the
+    reference's own results on the committed fixtures) on the same blast at
+    n^3, FP32, with every host core (OpenMP): one warm-up step, then steps
+    until budget_s.  Returns (zone-updates/s, steps, seconds, threads)."""
+    from _cases import blast_fd
+    from oracle import cpu
+
+    cfg, prm, rv, s = blast_fd(n=n, dtype=np.float32, t_end=10.0)
+    P = np.ascontiguousarray(s.astype(np.float32))
+    cpu.fd_run(P, cfg, prm, max_steps=1)
+    steps = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and steps < max_steps:
+        cpu.fd_run(P, cfg, prm, max_steps=1)
+        steps += 1
+    dt = time.perf_counter() - t0
+    return n ** 3 * steps / dt, steps, dt, cpu.threads()
+
+
+def cpu_baseline_fd(budget_s=15.0, n=64):
+    v, steps, dt, threads = cpu_fd_sample(n, budget_s)
+    return {"value": v, "unit": "zone-updates/s", "cores": threads, "kind": "port",
+            "sample": "compiled restatement of the reference's FD step (C++17, OpenMP, %d threads), "
+                      "blast %d^3 FP32, %d steps in %.1f s" % (threads, n, steps, dt)}
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    from _cases import blast_fd
+    from astronomix_gb300 import _native
+    from astronomix_gb300.time_integration import get_plan
+    from astronomix_gb300.replicas import replica_throughput
+
+    dev_index = torch.cuda.current_device()
+    n = args.n
+    cfg, prm, rv, s = blast_fd(n=n, dtype=np.float32, t_end=1e9)
+    s = s.astype(np.float32)
+    p = _native.make_params(prm)
+    plan = get_plan(cfg, rv, s.shape, np.float32)
+    stream = torch.cuda.current_stream()
+    st = stream.cuda_stream
+    state = torch.from_numpy(s).cuda()
+    plan.reset(st)
+
+    # warm-up: W steps
+    for _ in range(max(args.warmup, 3)):
+        plan.run_async(state.data_ptr(), p, 1, st)
+    torch.cuda.synchronize()
+
+    # timed: K steps, one CUDA-event pair per step; the plan also records an
+    # event after every launch (per-kernel durations for the roofline)
+    K = args.steps
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    plan.profile(True)
+    plan.profile_read(reset=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(dev_index) as clk:
+        for i in range(K):
+            starts[i].record(stream)
+            plan.run_async(state.data_ptr(), p, 1, st)
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    prof = plan.profile_read(reset=True)
+    plan.profile(False)
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_s = sum(step_ms) / 1e3
+    info = plan.run(state.data_ptr(), p, 0, st)
+    status = info.status
+    value = replica_throughput(n ** 3 * K, total_s)
+    total_s_max = max_over_ranks(total_s, world)
+    launches = int(sum(v[1] for v in prof.values()))
+    kernels = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / max(1e-30, sum(
+        w[0] for w in prof.values()))} for k, v in prof.items() if v[1]}
+
+    # ---- roofline of the dominant kernel, k_weno (x, y, z launches together)
+    weno_ms = sum(prof[k][0] for k in ("weno_x", "weno_y", "weno_z"))
+    weno_launches = sum(prof[k][1] for k in ("weno_x", "weno_y", "weno_z"))
+    weno_s = weno_ms / 1e3 / max(1, weno_launches)
+    peak, peak_src = hbm_peak()
+    achieved = WENO_BYTES_PER_CELL * n ** 3 / weno_s / 1e9
+    weno_prof = load_traffic("k_weno_fd_blast256_fp32") or {}
+    traffic = weno_prof.get("dram_bytes_per_launch")
+    fp32_peak = _native.probe_fp32_fma(st)
+    flop_per_cell = weno_prof.get("fp32_flop_per_cell")
+    compute = None
+    if flop_per_cell:
+        tf = flop_per_cell * n ** 3 / weno_s / 1e12
+        compute = {"achieved": tf, "peak": fp32_peak, "unit": "TFLOP/s", "frac": tf / fp32_peak,
+                   "flop_per_cell_per_launch": flop_per_cell,
+                   "note": "FP32 flops counted by ncu (fadd + fmul + 2 ffma) per k_weno launch / cells; "
+                           "peak = amx_probe_fp32_fma (register-only FMA chains on every SM)"}
+
+    # ---- end to end through the C ABI with host buffers (pinned)
+    host = torch.from_numpy(s.copy()).pin_memory()
+    host_out = torch.empty_like(host).pin_memory()
+    dev2 = torch.empty_like(state)
+    nbytes = host.numel() * host.element_size()
+    Ke = max(3, min(K, 10))
+    es = [torch.cuda.Event(enable_timing=True) for _ in range(Ke)]
+    ee = [torch.cuda.Event(enable_timing=True) for _ in range(Ke)]
+    plan.reset(st)
+    for i in range(Ke):
+        es[i].record(stream)
+        dev2.copy_(host, non_blocking=True)
+        plan.run_async(dev2.data_ptr(), p, 1, st)
+        host_out.copy_(dev2, non_blocking=True)
+        ee[i].record(stream)
+    torch.cuda.synchronize()
+    e2e_s = sum(a.elapsed_time(b) for a, b in zip(es, ee)) / 1e3
+    e2e_value = replica_throughput(n ** 3 * Ke, e2e_s)
+    del dev2, host, host_out
+
+    # ---- FP64: the same kernels in double precision (a few steps)
+    cfg64, prm64, rv64, s64 = blast_fd(n=n, dtype=np.float64, t_end=1e9)
+    plan64 = get_plan(cfg64, rv64, s64.shape, np.float64)
+    st64 = torch.from_numpy(s64.astype(np.float64)).cuda()
+    plan64.reset(st)
+    plan64.run_async(st64.data_ptr(), p, 1, st)
+    K64 = 3
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    plan64.run_async(st64.data_ptr(), p, K64, st)
+    b.record(stream)
+    torch.cuda.synchronize()
+    fp64_value = n ** 3 * K64 / (a.elapsed_time(b) / 1e3)
+    del st64
+
+    # ---- accuracy: full runs to t_end = 0.02 in FP32 and FP64 from the same state
+    l1 = None
+    if not args.no_l1:
+        res, steps_l1 = {}, {}
+        for name, dt in (("fp32", np.float32), ("fp64", np.float64)):
+            c_, pr_, rv_, s_ = blast_fd(n=n, dtype=dt, t_end=0.02)
+            pl = get_plan(c_, rv_, s_.shape, dt)
+            d_ = torch.from_numpy(s_.astype(dt)).cuda()
+            pl.reset(st)
+            inf = pl.run(d_.data_ptr(), _native.make_params(pr_), 1 << 40, st)
+            res[name] = d_[0].double()
+            steps_l1[name] = [inf.steps, inf.t, inf.status]
+            del d_
+        l1 = {"rel_l1_density": float((res["fp32"] - res["fp64"]).abs().sum() / res["fp64"].abs().sum()),
+              "t_end": 0.02, "runs": steps_l1}
+        del res
+
+    # ---- secondary workloads
+    ot = None if args.no_ot else time_orszag_tang()
     arena = {}
     if not args.no_arena:
         arena = {"fd_blast_fp32": time_arena("fd"), "fv_lf_blast_fp32": time_arena("fv"),
-                 "fd_blast_fp32_vs_fp64": fd_precision(), "fd_blast_forcing_wind_fp32": time_fd_sources(),
-                 "fv_split_hllc_blast_fp32": time_arena("fv_split")}
+                 "fd_blast_forcing_wind_fp32": time_fd_sources(), "fv_split_hllc_blast_fp32": time_arena("fv_split")}
         arena["fd_blast_forcing_wind_fp32"]["overhead_vs_plain"] = (
             arena["fd_blast_forcing_wind_fp32"]["s_per_step"] / arena["fd_blast_fp32"]["s_per_step"] - 1.0)
     ensemble = None if args.no_ensemble else time_ensemble()
@@ -850,9 +937,9 @@ def run_ours(args, rank, world):
 
     if rank != 0:
         return
-    cpu = None
-    if not args.no_cpu_baseline:
-        cpu = cpu_baseline_oracle()
+    cpu = None if args.no_cpu_baseline else cpu_baseline_fd()
+    config = workload_config(n)
+    config["parallelism"] = "replicas" if world > 1 else "single"
     line = {
         "metric": METRIC,
         "value": value,
@@ -866,25 +953,27 @@ def run_ours(args, rank, world):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "grid": [n, n], "precision": "fp32 fields, fp64 dt/time",
-                   "l2": "flushed between timed steps (512 MB write); state 7.3 MB",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": config,
         "e2e": {"value": e2e_value, "unit": "zone-updates/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes},
-        "gpu_launches": K,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "note": "algorithmic %.0f B/zone-update (k=%.2f fixed-point iterations), peak %s" % (
-                         bpz, k_mean, peak_src)},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_weno (x, y, z)", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "note": "algorithmic %.1f B/cell per launch, %.3f ms average launch, peak %s; the kernel "
+                             "is bound by FP32 issue, see compute" % (WENO_BYTES_PER_CELL, 1e3 * weno_s, peak_src),
+                     "compute": compute,
+                     "step": {"algorithmic_bytes_per_zone_update": FD_STEP_BYTES_PER_ZU,
+                              "achieved_gbs": FD_STEP_BYTES_PER_ZU * value / 1e9,
+                              "frac": FD_STEP_BYTES_PER_ZU * value / 1e9 / peak}},
+        "kernels": kernels,
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "fp64_value": fp64_value,
         "fp32_over_fp64": value / fp64_value,
-        "l1_err_vs_fp64": l1,
-        "l1_t": t_cmp,
-        "l1_steps": [infoA.steps, infoB.steps],
-        "fused_multistep_value": n * n * K / (fused_ms / 1e3),
-        "magnetic_iterations_mean": k_mean,
+        "l1_err_vs_fp64": l1["rel_l1_density"] if l1 else None,
+        "l1": l1,
+        "fp32_fma_peak_tflops": fp32_peak,
+        "fv_orszag_tang_512_fp32": ot,
         "reference_published_workloads": arena,
         "ensemble_fp32": ensemble,
         "adjoint_fp32": adjoint,
@@ -897,7 +986,7 @@ def run_ours(args, rank, world):
 def main():
     args = parse()
     if args.case:
-        run_case(args.case)
+        run_case(args.case, args.n)
         return
     rank, world = dist_setup(args)
     if args.impl == "reference":

@@ -142,6 +142,26 @@ typedef struct amx_plan amx_plan;
  * `max_history` (>= 0) sizes the per-step dt / iteration record. */
 int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out);
 int amx_plan_destroy(amx_plan* plan);
+/* No counterpart in the reference.  Limits of the FV persistent kernel:
+ * the cap on magnetic fixed-point iterations per update (the reference's
+ * 1000, _magnetic_field_update.py:141; reaching it sets
+ * AMX_ERR_NOT_CONVERGED) and the polls a block makes at a grid barrier
+ * before it gives up with AMX_ERR_TIMEOUT (2^24).  0 restores a default.
+ * For tests of the failure paths and for callers that want an earlier
+ * timeout; AMX_ERR_UNSUPPORTED for an FD plan (no fixed point, no barrier). */
+int amx_plan_set_limits(amx_plan* plan, int32_t max_fixed_point_iterations, int64_t barrier_spin_limit);
+/* No counterpart in the reference.  Per-kernel timing of the FD step: with
+ * amx_plan_profile(plan, 1), every amx_run / amx_run_until / amx_run_async
+ * step of an FD plan records a CUDA event after each of its launches on the
+ * caller's stream and waits for the step's last event (so steps no longer
+ * overlap host work); amx_plan_profile_read copies, per kernel kind, the
+ * summed milliseconds and the launch counts since the last reset into
+ * ms[n] / launches[n] (either may be null): 0 CFL, 1 stage prep, 2-4 WENO
+ * x / y / z, 5 edge EMF, 6 EMF averages, 7 wind source, 8 stage update,
+ * 9 finalize, 10 turbulent forcing.  AMX_ERR_UNSUPPORTED for an FV plan
+ * (one persistent launch per step). */
+int amx_plan_profile(amx_plan* plan, int32_t enable);
+int amx_plan_profile_read(amx_plan* plan, double* ms, int64_t* launches, int32_t n, int32_t reset);
 /* Bytes of device workspace the plan holds. */
 int amx_plan_workspace_bytes(const amx_plan* plan, size_t* bytes);
 /* Resets time, step counters, history and status to zero (stream-ordered). */
@@ -235,7 +255,12 @@ int amx_status(amx_plan* plan, int32_t* status_host, int32_t clear, void* stream
  * more return AMX_ERR_TOO_LARGE (2D MHD fits up to 362^2 cells in FP32 and
  * 255^2 in FP64; 3D MHD up to 49^3 / 39^3).  The first call on each device
  * resolves the array's device address; make it before any stream capture.
- * Fills *info (and synchronises) when info is non-null. */
+ * Fills *info (and synchronises) when info is non-null; since a stream that
+ * is being captured may not be synchronised, such a call on a capturing
+ * stream returns AMX_ERR_INVALID_ARG without launching anything.  Accepts what amx_plan_create accepts for the FV
+ * scheme (including VAN_ALBADA_PP), except self_gravity, turbulent_forcing
+ * and stellar_wind (AMX_ERR_UNSUPPORTED: they need cuFFT work between the
+ * kernel's phases) and FD configurations. */
 int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_params* prm, int64_t max_steps,
                        amx_run_info* info, void* stream);
 

@@ -634,6 +634,11 @@ def _norm0(a):
     return xp.sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2])
 
 
+# the fixed point's iteration cap (_magnetic_field_update.py:141); a module
+# constant so that a test can lower it to follow a capped GPU run
+MAX_FIXED_POINT_ITERATIONS = 1000
+
+
 def magnetic_update(B, gas, dx, dt, config, rv, return_iterations=False):
     """_finite_volume/_magnetic_update/_magnetic_field_update.py:37-242.
 
@@ -679,7 +684,7 @@ def magnetic_update(B, gas, dx, dt, config, rv, return_iterations=False):
     Bk, vk, Bkp1, vkp1, it = B0, v0, B1, v1, 0
     while True:
         change = max(xp.to_float(xp.amax(_norm0(Bk - Bkp1))), xp.to_float(xp.amax(_norm0(vk - vkp1))))
-        if not ((change > tol) and (it < 1000)):
+        if not ((change > tol) and (it < MAX_FIXED_POINT_ITERATIONS)):
             break
         Bk, vk = Bkp1, vkp1
         if config.fv_magnetic_integrator == IMPLICIT_MIDPOINT:

@@ -1,0 +1,128 @@
+"""The oracle against results of the reference's own code (tests/golden/reference_fixtures.npz).
+
+tests/golden/make_reference_fixtures.py ran leo1200/astronomix, unchanged, on
+a NumPy stand-in for JAX: whole `time_integration` calls and single
+hot-path functions on the seeded cases of tests/golden/reference_cases.py.
+Here the oracle recomputes each case and must agree to 1e-12 relative (FP64).
+This pins the oracle to the reference; the GPU parity tests pin the CUDA path
+to the oracle (and test_reference_fixtures_gpu.py to the fixtures directly).
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+import reference_cases as rc  # noqa: E402
+from oracle import driver, fv as ofv, fd as ofd  # noqa: E402
+from _cases import rel_err, PERIODIC_2D  # noqa: E402
+
+FIX = np.load(os.path.join(HERE, "golden", "reference_fixtures.npz"))
+TOL = 1e-12
+
+
+def _digest(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(np.asarray(a, dtype=np.float64)).tobytes()).hexdigest()[:16]
+
+
+@pytest.mark.parametrize("name", sorted(rc.RUN_CASES))
+def test_oracle_time_integration_matches_reference(name):
+    cfg, prm, rv, s = rc.RUN_CASES[name]()
+    assert str(FIX[name + "/input_digest"]) == _digest(s), "the seeded input changed since the fixtures were made"
+    got = driver.time_integration(np.array(s, dtype=np.float64), cfg, prm, rv)
+    ref = FIX[name + "/output"]
+    assert got.shape == ref.shape
+    assert rel_err(got, ref) < TOL
+
+
+def _hydro2d(riemann=0, limiter=0, n=16):
+    from astronomix_gb300 import SimulationConfig, finalize_config, get_registered_variables, PERIODIC_ROLL
+    cfg = SimulationConfig(dimensionality=2, box_size=1.0, num_cells=n, riemann_solver=riemann, limiter=limiter,
+                           boundary_settings=PERIODIC_2D, boundary_handling=PERIODIC_ROLL)
+    cfg = finalize_config(cfg, (4, n, n))
+    return cfg, get_registered_variables(cfg)
+
+
+def _rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("name,rs,d", [("riemann_hll", 0, 1), ("riemann_hllc", 1, 2), ("riemann_hllc_lm", 2, 1),
+                                       ("riemann_lax_friedrichs", 3, 1)])
+def test_oracle_riemann_solvers(name, rs, d):
+    cfg, rv = _hydro2d(riemann=rs)
+    got = ofv.riemann_solver(rc.prim2d(1), rc.prim2d(2), rc.prim2d(3), 5 / 3, cfg, rv, d)
+    assert rel_err(got, FIX[name + "/output"]) < TOL
+
+
+def test_oracle_limited_gradients():
+    from astronomix_gb300 import MINMOD, OSHER, DOUBLE_MINMOD, SUPERBEE, VAN_ALBADA
+    P = rc.prim2d(4)
+    got = []
+    for lim in (MINMOD, OSHER, DOUBLE_MINMOD, SUPERBEE, VAN_ALBADA):
+        cfg, rv = _hydro2d(limiter=lim)
+        for axis in (1, 2):
+            got.append(ofv.limited_gradients(P, cfg, axis))
+    ref = FIX["limited_gradients/output"]
+    for g, r in zip(got, ref):
+        assert _rel(g, r) < TOL
+
+
+def test_oracle_magnetic_update():
+    from astronomix_gb300 import SimulationConfig, finalize_config, get_registered_variables, PERIODIC_ROLL
+    cfg = SimulationConfig(mhd=True, dimensionality=2, box_size=1.0, num_cells=16, boundary_settings=PERIODIC_2D,
+                           boundary_handling=PERIODIC_ROLL)
+    cfg = finalize_config(cfg, (7, 16, 16))
+    rv = get_registered_variables(cfg)
+    B, gas = rc.mag2d(5)
+    Bn, gn = ofv.magnetic_update(B, gas, cfg.grid_spacing, 1e-3, cfg, rv)
+    assert rel_err(np.concatenate([gn, Bn]), FIX["magnetic_update_2d/output"]) < TOL
+
+
+def test_oracle_cfl_estimates():
+    cfg, rv = _hydro2d()
+    dt = ofv.cfl_time_step(rc.prim2d(6), cfg.grid_spacing, 1.0, 5 / 3, cfg, rv, 0.4)
+    assert float(dt) == pytest.approx(float(FIX["cfl_fv_2d/output"]), rel=1e-14)
+    P = ofd.prim_from_cons(rc.cons3d_mhd(7), 1e-14, 1e-14, 5 / 3)
+    dt = ofd.cfl_time_step_fd(P, 1 / 8, 1.0, 5 / 3, 1.5, 1e-14, 1e-14)
+    assert float(dt) == pytest.approx(float(FIX["cfl_fd/output"]), rel=1e-14)
+
+
+def test_oracle_weno_fluxes():
+    U = rc.cons3d_mhd(8)
+    ref = FIX["weno_flux/output"]
+    for k in range(3):
+        assert _rel(ofd.weno_flux(U, k + 1, 1e-14, 1e-14, 5 / 3), ref[k]) < TOL, k
+
+
+def test_oracle_eigenvalues():
+    assert _rel(ofd.all_lambdas(rc.cons3d_mhd(9), 5 / 3, 1e-14, 1e-14), FIX["eigen_lambdas/output"]) < TOL
+
+
+def test_oracle_constrained_transport_rhs():
+    U = rc.cons3d_mhd(10)
+    Fx, Fy, Fz = rc.fluxes3d(10)
+    got = np.stack(ofd.ct_rhs(U, Fx, Fy, Fz, 0.01, 0.01, 0.01))
+    assert _rel(got, FIX["constrained_transport_rhs/output"]) < TOL
+
+
+def test_oracle_positivity_and_cell_centre_fields():
+    got = ofd.enforce_positivity(rc.cons3d_mhd(11), 5 / 3, 1.1, 0.9)
+    assert _rel(got, FIX["enforce_positivity/output"]) < TOL
+    bx, by, bz = rc.faces3d(12)
+    got = ofd.update_cell_center_fields(rc.cons3d_mhd(12), bx, by, bz)
+    assert _rel(got, FIX["update_cell_center_fields/output"]) < TOL
+
+
+def test_oracle_fd_step():
+    U = rc.cons3d_mhd(13)
+    bx, by, bz = rc.faces3d(13)
+    P = np.concatenate([ofd.prim_from_cons(U, 1e-14, 1e-14, 5 / 3), np.stack([bx, by, bz])])
+    got = ofd.evolve_state_fd(P, 2e-3, 5 / 3, 1 / 8, 1e-14, 1e-14)
+    assert rel_err(got, FIX["evolve_state_fd/output"]) < TOL
