@@ -233,7 +233,7 @@ class Plan:
               "amx_plan_set_limits")
 
     FD_KERNELS = ("cfl", "prep", "weno_x", "weno_y", "weno_z", "emf", "emf_avg", "wind", "update", "finalize",
-                  "forcing")
+                  "forcing", "advance")
 
     def profile(self, enable=True):
         """Per-kernel CUDA-event timing of the FD step (FD plans only)."""

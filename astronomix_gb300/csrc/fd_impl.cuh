@@ -1,8 +1,8 @@
 // Finite-difference WENO-CT MHD step: kernels and their typed launchers.
 //
 // One time step = 1 CFL reduction + 5 SSPRK(5,4) stages x 7 sweeps + 1
-// finalize sweep, all stream-ordered launches that read dt from the device
-// control block (no host round trip per step).  Stage s:
+// finalize sweep + the time advance (38 launches), all stream-ordered, reading
+// dt from the device control block (no host round trip per step).  Stage s:
 //
 //   prep      q <- positivity(q); qc <- update_cell_center_fields(q, b)
 //   weno x/y/z   interface fluxes of qc; acc += F[i+1/2] - F[i-1/2];
@@ -34,6 +34,21 @@ static __constant__ double kFIN[5] = {-2.081261929715610e-02, 0.0, 0.51723167208
 
 constexpr int kThreads = 256;
 
+// The pointwise sweeps run one thread per cell on a 3D grid: blocks of 32
+// (z) x 8 (y) threads, grid (n/32, n/8, n) -- (i, j, k) come from the block
+// and thread indices, with no integer division.
+constexpr int kSweepZ = 32, kSweepY = 8;
+inline dim3 sweep_grid(int n) { return dim3((n + kSweepZ - 1) / kSweepZ, (n + kSweepY - 1) / kSweepY, n); }
+inline dim3 sweep_block() { return dim3(kSweepZ, kSweepY, 1); }
+__device__ __forceinline__ bool sweep_cell(int n, int* i, int* j, int* k, long long* c) {
+  *k = blockIdx.x * kSweepZ + threadIdx.x;
+  *j = blockIdx.y * kSweepY + threadIdx.y;
+  *i = blockIdx.z;
+  if (*k >= n || *j >= n) return false;
+  *c = cidx(*i, *j, *k, n);
+  return true;
+}
+
 template <typename T>
 struct Bufs {
   T* P;    // state (prim, 11 rows)
@@ -41,7 +56,7 @@ struct Bufs {
   T* Q;    // 8
   T* QF;   // 8
   T* QC;   // 8
-  T* ACC;  // 8
+  T* ACC;  // 3 x 8: the flux differences of the x, y and z interfaces
   T* B;    // 3  current face fields
   T* BF;   // 3  final accumulator of the faces
   T* M;    // 6  CT-corrected face fluxes: By_fx Bz_fx Bx_fy Bz_fy Bx_fz By_fz
@@ -153,7 +168,9 @@ __global__ void __launch_bounds__(kThreads) k_prep(Bufs<T> b, int stage) {
   const int n = a.n;
   const T* faces = (stage == 0) ? b.P + 8 * nc : b.B;
   const T f0 = T(kFIN[0]);
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
+  int i, j, k;
+  long long c;
+  if (sweep_cell(n, &i, &j, &k, &c)) {
     T U[8];
     if (stage == 0) {
       T P[8];
@@ -179,8 +196,6 @@ __global__ void __launch_bounds__(kThreads) k_prep(Bufs<T> b, int stage) {
       b.Q[RHO * nc + c] = U[RHO];
       b.Q[EN * nc + c] = U[EN];
     }
-    int i, j, k;
-    decompose(c, n, &i, &j, &k);
     ucc(U, faces, faces + nc, faces + 2 * nc, i, j, k, n);
 #pragma unroll
     for (int r = 0; r < 8; ++r) b.QC[r * nc + c] = U[r];
@@ -200,45 +215,97 @@ enum : int {
   kSV = 23
 };
 
+// index of a permuted-frame conserved row in the 7-vectors (Bx dropped):
+// rho mx my mz E By Bz -> 0..6, Bx -> -1
+__host__ __device__ constexpr int c7(int row) { return row < BX ? row : (row == BX ? -1 : row - 1); }
+
 // Tile of A cells along the flux axis x 32 lanes across it.  Every staged
 // cell (A + 6 with the halo of 3) costs a flux and an eigensystem; every
 // thread owns whole interfaces.  Shared memory is a structure of arrays
 // with a row pitch of 33 values, so that a warp reading 32 lanes of one row
 // (the interface sweep) and a warp reading 32 cells of one lane (the
 // staging and the store of the z-axis tile) are both free of bank
-// conflicts.  FP32: A = 47, 384 threads (the 48 x 32 interfaces are four per
-// thread; 168 registers a thread, 12 warps per SM; the largest tile that
-// fits, 212 KB).  Measured on the 256^3 blast, s/step: 0.0499 (47, 384),
-// 0.0504 (32, 384), 0.0511 (32, 352), 0.0577 (31, 256: 255 registers,
-// 8 warps).  FP64: A = 15, 256 threads.
+// conflicts.  FP32: A = 11, 128 threads (the 12 x 32 interfaces are three
+// per thread), three blocks per SM (168 registers a thread, 63 KB of shared
+// memory a block), so that one block's staging loads and stores overlap the
+// others' arithmetic.  Measured on the 256^3 blast, WENO x / y / z ms per
+// launch: 1.50 / 1.49 / 1.60 (11, 128, 3 blocks), 1.53 / 1.51 / 1.56 (23,
+// 192, 2), 1.64 / 1.63 / 1.69 (47, 384, 1).  FP64: A = 15, 256 threads,
+// one block.
 #ifndef AMX_WENO_A32
-#define AMX_WENO_A32 47
+#define AMX_WENO_A32 11
 #endif
 #ifndef AMX_WENO_T32
-#define AMX_WENO_T32 384
+#define AMX_WENO_T32 128
+#endif
+#ifndef AMX_WENO_B32
+#define AMX_WENO_B32 3
 #endif
 template <typename T> struct WenoTile {
   static constexpr int A = sizeof(T) == 4 ? AMX_WENO_A32 : 15;
   static constexpr int THREADS = sizeof(T) == 4 ? AMX_WENO_T32 : 256;
+  static constexpr int BLOCKS = sizeof(T) == 4 ? AMX_WENO_B32 : 1;  // resident blocks per SM
   static constexpr int L = 32;
   static constexpr int LP = 33;
   static constexpr int AH = A + 6;
 };
 
+// Shared memory of a tile.  FP64: kSV scalar rows.  FP32: the flux and the
+// state component a characteristic projection pairs with it as 7 float2
+// rows (F_c, U_c), then 9 scalar rows (Bx, the eigenvector-block inputs,
+// the wave speeds): the same 23 values a cell, laid out for the paired FP32
+// arithmetic.  Then the interface fluxes, 7 rows.
 template <typename T>
 constexpr size_t weno_smem() {
   using W = WenoTile<T>;
   return sizeof(T) * ((size_t)kSV * W::AH * W::LP + (size_t)7 * (W::A + 1) * W::LP);
 }
+constexpr int kSX = 9;  // FP32 scalar rows: 0 Bx, 1-5 eigenvector-block inputs, 6-8 cf ca cs
 
+// Views of a tile's staged cells in either layout.
+template <typename T> struct WenoStage;
+template <> struct WenoStage<double> {
+  double* S;
+  int AH, LP;
+  __device__ double& v(int row, int ai, int li) const { return S[((size_t)row * AH + ai) * LP + li]; }
+  __device__ void store(const double* out, int ai, int li) const {
+#pragma unroll
+    for (int k = 0; k < kSV; ++k) v(k, ai, li) = out[k];
+  }
+  __device__ double U(int r, int ai, int li) const { return v(SV_U + r, ai, li); }
+  __device__ double F(int c, int ai, int li) const { return v(SV_F + c, ai, li); }
+  __device__ double EV(int k, int ai, int li) const { return v(SV_EV + k, ai, li); }
+  __device__ double C(int k, int ai, int li) const { return v(SV_C + k, ai, li); }
+};
+template <> struct WenoStage<float> {
+  float2* P;  // [7][AH][LP] (F_c, U_c)
+  float* X;   // [kSX][AH][LP]
+  int AH, LP;
+  __device__ float2& p(int c, int ai, int li) const { return P[((size_t)c * AH + ai) * LP + li]; }
+  __device__ float& x(int k, int ai, int li) const { return X[((size_t)k * AH + ai) * LP + li]; }
+  __device__ void store(const float* out, int ai, int li) const {
+#pragma unroll
+    for (int c = 0; c < 7; ++c) p(c, ai, li) = make_float2(out[SV_F + c], out[SV_U + (c < 5 ? c : c + 1)]);
+    x(0, ai, li) = out[SV_U + BX];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) x(1 + k, ai, li) = out[SV_EV + k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) x(6 + k, ai, li) = out[SV_C + k];
+  }
+  __device__ float U(int r, int ai, int li) const { return r == BX ? x(0, ai, li) : p(c7(r), ai, li).y; }
+  __device__ float F(int c, int ai, int li) const { return p(c, ai, li).x; }
+  __device__ float EV(int k, int ai, int li) const { return x(1 + k, ai, li); }
+  __device__ float C(int k, int ai, int li) const { return x(6 + k, ai, li); }
+};
+
+// g mod n for g in [-n, n + span): a few compares instead of an integer
+// division (the tiles' halo reaches 3 cells below 0 and A + 2 above n - 1)
 __device__ __forceinline__ int pmod(int g, int n) {
-  int r = g % n;
-  return r < 0 ? r + n : r;
+  if (g < 0) g += n;
+  while (g >= n) g -= n;
+  return g;
 }
 
-// index of a permuted-frame conserved row in the 7-vectors (Bx dropped):
-// rho mx my mz E By Bz -> 0..6, Bx -> -1
-__host__ __device__ constexpr int c7(int row) { return row < BX ? row : (row == BX ? -1 : row - 1); }
 
 // Everything a staged cell needs, with the arithmetic of _mhd_flux_x
 // (_fluxes.py:23-69 via primitive_state_from_conserved), of the per-cell
@@ -478,19 +545,100 @@ __device__ __forceinline__ void weno_mode(const EigIF<T>& e, const T (&dF)[5][7]
     if (RM & (1u << c)) Fi[c] = Fi[c] + R[c] * Fs;
 }
 
+// ---- paired FP32 arithmetic (fma.rn.f32x2 and friends on sm_100+): two
+// FP32 operations per issue slot, each rounded like its scalar form
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b) {  // a - b, exactly as two FSUBs
+  return __ffma2_rn(b, f2(-1.f, -1.f), a);
+}
+
+// The two WENO interpolants of one characteristic field, weno_phi of
+// (second, third) as one pair (_weno.py:186-228).
+__device__ __forceinline__ float2 weno_phi2(float2 a, float2 b, float2 c, float2 d) {
+  const float2 k13 = f2(13.f, 13.f), k3 = f2(3.f, 3.f), eps = f2(1e-8f, 1e-8f);
+  const float2 t0 = f2sub(a, b), u0 = __ffma2_rn(b, f2(-3.f, -3.f), a);
+  const float2 IS0 = __ffma2_rn(k13, __fmul2_rn(t0, t0), __fmul2_rn(k3, __fmul2_rn(u0, u0)));
+  const float2 t1 = f2sub(b, c), u1 = __fadd2_rn(b, c);
+  const float2 IS1 = __ffma2_rn(k13, __fmul2_rn(t1, t1), __fmul2_rn(k3, __fmul2_rn(u1, u1)));
+  const float2 t2 = f2sub(c, d), u2 = __ffma2_rn(c, k3, f2(-d.x, -d.y));
+  const float2 IS2 = __ffma2_rn(k13, __fmul2_rn(t2, t2), __fmul2_rn(k3, __fmul2_rn(u2, u2)));
+  const float2 e0 = __fadd2_rn(eps, IS0), e1 = __fadd2_rn(eps, IS1), e2 = __fadd2_rn(eps, IS2);
+  const float2 s0 = __fmul2_rn(e0, e0), s1 = __fmul2_rn(e1, e1), s2 = __fmul2_rn(e2, e2);
+  const float2 al0 = f2(1.f / s0.x, 1.f / s0.y);
+  const float2 al1 = __fmul2_rn(f2(6.f, 6.f), f2(1.f / s1.x, 1.f / s1.y));
+  const float2 al2 = __fmul2_rn(k3, f2(1.f / s2.x, 1.f / s2.y));
+  float2 asum = __fadd2_rn(__fadd2_rn(al0, al1), al2);
+  asum = f2(fmaxf(asum.x, 1e-14f), fmaxf(asum.y, 1e-14f));
+  const float2 r = f2(1.f / asum.x, 1.f / asum.y);
+  const float2 w0 = __fmul2_rn(al0, r), w2 = __fmul2_rn(al2, r);
+  const float2 p = __fadd2_rn(__ffma2_rn(b, f2(-2.f, -2.f), a), c);
+  const float2 q = __fadd2_rn(__ffma2_rn(c, f2(-2.f, -2.f), b), d);
+  const float2 first = __fmul2_rn(__fmul2_rn(w0, p), f2(1.f / 3.f, 1.f / 3.f));
+  const float2 g = __fmul2_rn(__fadd2_rn(w2, f2(-0.5f, -0.5f)), q);
+  return __ffma2_rn(g, f2(1.f / 6.f, 1.f / 6.f), first);
+}
+
+// One characteristic field (weno_mode) with the stencil differences held as
+// (flux, state) pairs: each left-row coefficient multiplies both at once.
+template <int S>
+__device__ __forceinline__ void weno_mode2(const EigIF<float>& e, const float2 (&dd)[5][7], float alpha,
+                                           float (&Fi)[7]) {
+  constexpr unsigned LM = lmask<S>(), RM = rmask<S>();
+  float L[7];
+  L7<float, S>(e, L);
+  float2 dq[5];  // (L.dF_k, L.dq_k), halved
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    float2 acc = f2(0.f, 0.f);
+    bool first = true;
+#pragma unroll
+    for (int c = 0; c < 7; ++c) {
+      if (LM & (1u << c)) {
+        const float2 l = f2(L[c], L[c]);
+        acc = first ? __fmul2_rn(dd[k][c], l) : __ffma2_rn(dd[k][c], l, acc);
+        first = false;
+      }
+    }
+    dq[k] = acc;
+  }
+  // inputs of the two interpolants: second (d_k + alpha q_k, k = 0..3),
+  // third (d_k - alpha q_k, k = 4..1), interleaved as pairs
+  const float2 A = f2(fmaf(alpha, dq[0].y, dq[0].x), fmaf(-alpha, dq[4].y, dq[4].x));
+  const float2 B = f2(fmaf(alpha, dq[1].y, dq[1].x), fmaf(-alpha, dq[3].y, dq[3].x));
+  const float2 C = f2(fmaf(alpha, dq[2].y, dq[2].x), fmaf(-alpha, dq[2].y, dq[2].x));
+  const float2 D = f2(fmaf(alpha, dq[3].y, dq[3].x), fmaf(-alpha, dq[1].y, dq[1].x));
+  const float2 st = weno_phi2(A, B, C, D);
+  const float Fs = -st.x + st.y;
+  float R[7];
+  R7<float, S>(e, R);
+#pragma unroll
+  for (int c = 0; c < 7; ++c)
+    if (RM & (1u << c)) Fi[c] = Fi[c] + R[c] * Fs;
+}
+
 // Interface fluxes along axis D (0 = x, 1 = y, 2 = z), _weno.py:112-324,
 // with the flux difference into acc and the CT-corrected fluxes of the two
 // tangential field components (_constrained_transport.py:77-102) fused into
 // the store.
 template <typename T, int D>
-__global__ void __launch_bounds__(WenoTile<T>::THREADS, 1) k_weno(Bufs<T> b) {
+__global__ void __launch_bounds__(WenoTile<T>::THREADS, WenoTile<T>::BLOCKS) k_weno(Bufs<T> b) {
   using W = WenoTile<T>;
   constexpr int kA = W::A, kL = W::L, kLP = W::LP, kAH = W::AH, kT = W::THREADS;
   FD_ACTIVE_OR_RETURN(b.ctl);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* S = reinterpret_cast<T*>(smem_raw);        // [kSV][kAH][kLP]
-  T* FI = S + (size_t)kSV * kAH * kLP;          // [7][kA+1][kLP] (permuted frame)
-  auto sv = [&](int v, int ai, int li) -> T& { return S[((size_t)v * kAH + ai) * kLP + li]; };
+  WenoStage<T> st;
+  T* FI;  // [7][kA+1][kLP] (permuted frame)
+  if constexpr (sizeof(T) == 4) {
+    st.P = reinterpret_cast<float2*>(smem_raw);
+    st.X = reinterpret_cast<float*>(st.P + (size_t)7 * kAH * kLP);
+    FI = st.X + (size_t)kSX * kAH * kLP;
+  } else {
+    st.S = reinterpret_cast<T*>(smem_raw);
+    FI = st.S + (size_t)kSV * kAH * kLP;
+  }
+  st.AH = kAH;
+  st.LP = kLP;
   auto fi = [&](int c, int ii, int li) -> T& { return FI[((size_t)c * (kA + 1) + ii) * kLP + li]; };
   const FDArgs a = b.a;
   const T gamma = T(a.gamma), rhomin = T(a.rhomin), pgmin = T(a.pgmin);
@@ -524,8 +672,7 @@ __global__ void __launch_bounds__(WenoTile<T>::THREADS, 1) k_weno(Bufs<T> b) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) U[r] = b.QC[perm_row(D, r) * nc + c];
     weno_cell(U, gamma, rhomin, pgmin, floors, out);
-#pragma unroll
-    for (int v = 0; v < kSV; ++v) sv(v, ai, li) = out[v];
+    st.store(out, ai, li);
   }
   __syncthreads();
 
@@ -534,46 +681,15 @@ __global__ void __launch_bounds__(WenoTile<T>::THREADS, 1) k_weno(Bufs<T> b) {
 #pragma unroll 1
   for (int task = threadIdx.x; task < (kA + 1) * kL; task += kT) {
     const int li = task % kL, ii = task / kL;
-    // differences of the flux and the state over the stencil, and the base
-    // flux 1/12 (-F[i-1] + 7 F[i] + 7 F[i+1] - F[i+2])
-    T dF[5][7], dq[5][7], Fi[7];
-    {
-      T fp[7], qp[7], f1[7], f2[7], f3[7];
-#pragma unroll
-      for (int m = 0; m < 6; ++m) {
-        T f[7], q[7];
-#pragma unroll
-        for (int c = 0; c < 7; ++c) {
-          f[c] = sv(SV_F + c, ii + m, li);
-          q[c] = sv(SV_U + (c < 5 ? c : c + 1), ii + m, li);
-        }
-        if (m > 0) {
-#pragma unroll
-          for (int c = 0; c < 7; ++c) {
-            dF[m - 1][c] = f[c] - fp[c];
-            dq[m - 1][c] = q[c] - qp[c];
-          }
-        }
-#pragma unroll
-        for (int c = 0; c < 7; ++c) {
-          fp[c] = f[c];
-          qp[c] = q[c];
-          if (m == 1) f1[c] = f[c];
-          if (m == 2) f2[c] = f[c];
-          if (m == 3) f3[c] = f[c];
-          if (m == 4) Fi[c] = T(1.0 / 12.0) * (-f1[c] + T(7) * f2[c] + T(7) * f3[c] - f[c]);
-        }
-      }
-    }
     // alpha_s = max |lambda_s| over the six stencil cells (cell centred)
     T al[7];
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
-      const T vx = sv(SV_EV + 1, ii + m, li), cf = sv(SV_C + 0, ii + m, li), ca = sv(SV_C + 1, ii + m, li),
-              cs = sv(SV_C + 2, ii + m, li);
+      const T vx = st.EV(1, ii + m, li), cf = st.C(0, ii + m, li), ca = st.C(1, ii + m, li),
+              cs = st.C(2, ii + m, li);
       const T lam[7] = {vx - cf, vx - ca, vx - cs, vx, vx + cs, vx + ca, vx + cf};
 #pragma unroll
-      for (int s = 0; s < 7; ++s) al[s] = (m == 0) ? Num<T>::abs_(lam[s]) : jmax(al[s], Num<T>::abs_(lam[s]));
+      for (int s = 0; s < 7; ++s) al[s] = (m == 0) ? Num<T>::abs_(lam[s]) : wmax(al[s], Num<T>::abs_(lam[s]));
     }
     // eigenvector blocks from cells i (row ii+2) and i+1 (row ii+3)
     EigIF<T> e;
@@ -581,28 +697,73 @@ __global__ void __launch_bounds__(WenoTile<T>::THREADS, 1) k_weno(Bufs<T> b) {
       T cL[5], cR[5];
 #pragma unroll
       for (int k = 0; k < 5; ++k) {
-        cL[k] = sv(SV_EV + k, ii + 2, li);
-        cR[k] = sv(SV_EV + k, ii + 3, li);
+        cL[k] = st.EV(k, ii + 2, li);
+        cR[k] = st.EV(k, ii + 3, li);
       }
-      eig_interface(cL, cR, sv(SV_U + BX, ii + 2, li), sv(SV_U + BY, ii + 2, li), sv(SV_U + BZ, ii + 2, li),
-                    sv(SV_U + BX, ii + 3, li), sv(SV_U + BY, ii + 3, li), sv(SV_U + BZ, ii + 3, li), gamma, e);
+      eig_interface(cL, cR, st.U(BX, ii + 2, li), st.U(BY, ii + 2, li), st.U(BZ, ii + 2, li), st.U(BX, ii + 3, li),
+                    st.U(BY, ii + 3, li), st.U(BZ, ii + 3, li), gamma, e);
     }
-    weno_mode<T, 0>(e, dF, dq, al[0], Fi);
-    weno_mode<T, 1>(e, dF, dq, al[1], Fi);
-    weno_mode<T, 2>(e, dF, dq, al[2], Fi);
-    weno_mode<T, 3>(e, dF, dq, al[3], Fi);
-    weno_mode<T, 4>(e, dF, dq, al[4], Fi);
-    weno_mode<T, 5>(e, dF, dq, al[5], Fi);
-    weno_mode<T, 6>(e, dF, dq, al[6], Fi);
+    // the base flux 1/12 (-F[i-1] + 7 F[i] + 7 F[i+1] - F[i+2]) and the
+    // differences of the flux and the state over the stencil
+    T Fi[7];
+#pragma unroll
+    for (int c = 0; c < 7; ++c)
+      Fi[c] = T(1.0 / 12.0) * (-st.F(c, ii + 1, li) + T(7) * st.F(c, ii + 2, li) + T(7) * st.F(c, ii + 3, li) -
+                               st.F(c, ii + 4, li));
+    if constexpr (sizeof(T) == 4) {
+      float2 dd[5][7];  // (F[m+1] - F[m], U[m+1] - U[m])
+#pragma unroll
+      for (int c = 0; c < 7; ++c) {
+        float2 prev = st.p(c, ii, li);
+#pragma unroll
+        for (int m = 1; m < 6; ++m) {
+          const float2 cur = st.p(c, ii + m, li);
+          dd[m - 1][c] = f2sub(cur, prev);
+          prev = cur;
+        }
+      }
+      weno_mode2<0>(e, dd, al[0], Fi);
+      weno_mode2<1>(e, dd, al[1], Fi);
+      weno_mode2<2>(e, dd, al[2], Fi);
+      weno_mode2<3>(e, dd, al[3], Fi);
+      weno_mode2<4>(e, dd, al[4], Fi);
+      weno_mode2<5>(e, dd, al[5], Fi);
+      weno_mode2<6>(e, dd, al[6], Fi);
+    } else {
+      T dF[5][7], dq[5][7];
+#pragma unroll
+      for (int c = 0; c < 7; ++c) {
+        const int r = c < 5 ? c : c + 1;
+        T fp = st.F(c, ii, li), qp = st.U(r, ii, li);
+#pragma unroll
+        for (int m = 1; m < 6; ++m) {
+          const T f = st.F(c, ii + m, li), q = st.U(r, ii + m, li);
+          dF[m - 1][c] = f - fp;
+          dq[m - 1][c] = q - qp;
+          fp = f;
+          qp = q;
+        }
+      }
+      weno_mode<T, 0>(e, dF, dq, al[0], Fi);
+      weno_mode<T, 1>(e, dF, dq, al[1], Fi);
+      weno_mode<T, 2>(e, dF, dq, al[2], Fi);
+      weno_mode<T, 3>(e, dF, dq, al[3], Fi);
+      weno_mode<T, 4>(e, dF, dq, al[4], Fi);
+      weno_mode<T, 5>(e, dF, dq, al[5], Fi);
+      weno_mode<T, 6>(e, dF, dq, al[6], Fi);
+    }
 #pragma unroll
     for (int c = 0; c < 7; ++c) fi(c, ii, li) = Fi[c];
   }
   __syncthreads();
 
-  // ---- cells a0 .. a0+kA-1: flux difference into acc, CT-corrected fluxes at their faces
+  // ---- cells a0 .. a0+kA-1: the flux difference of this axis into its own
+  // buffer (a store, no read: the sum over axes is k_update's), the
+  // CT-corrected fluxes at their faces
   // lab rows of the two tangential B components whose fluxes CT corrects
   constexpr int T1 = (D == 0) ? BY : BX;
   constexpr int T2 = (D == 2) ? BY : BZ;
+  T* const acc = b.ACC + (size_t)D * 8 * nc;
   for (int task = threadIdx.x; task < kA * kL; task += kT) {
     int ci, li;
     if (D == 2) { ci = task % kA; li = task / kA; }
@@ -614,22 +775,16 @@ __global__ void __launch_bounds__(WenoTile<T>::THREADS, 1) k_weno(Bufs<T> b) {
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int k = c7(perm_row(D, r));
-      if (k < 0) {
-        if (D == 0) b.ACC[r * nc + c] = T(0);  // the x-flux of Bx vanishes
-        continue;
-      }
-      const T dF = fi(k, ci + 1, li) - fi(k, ci, li);
-      if (D == 0) b.ACC[r * nc + c] = dF;
-      else b.ACC[r * nc + c] = b.ACC[r * nc + c] + dF;
+      if (k < 0) continue;  // the flux of B along its own axis vanishes (k_update skips the row)
+      acc[r * nc + c] = fi(k, ci + 1, li) - fi(k, ci, li);
     }
     // c2f over cells i-1 .. i+2 (staged rows ci+2 .. ci+5) of B_d and v_t (lab frame)
-    const T Bn = c2f(sv(SV_U + BX, ci + 2, li), sv(SV_U + BX, ci + 3, li), sv(SV_U + BX, ci + 4, li),
-                     sv(SV_U + BX, ci + 5, li));
+    const T Bn = c2f(st.U(BX, ci + 2, li), st.U(BX, ci + 3, li), st.U(BX, ci + 4, li), st.U(BX, ci + 5, li));
     constexpr int m1 = perm_row_c(D, T1 - BX + MX) - MX, m2 = perm_row_c(D, T2 - BX + MX) - MX;
-    const T v1 = c2f(sv(SV_EV + 1 + m1, ci + 2, li), sv(SV_EV + 1 + m1, ci + 3, li),
-                     sv(SV_EV + 1 + m1, ci + 4, li), sv(SV_EV + 1 + m1, ci + 5, li));
-    const T v2 = c2f(sv(SV_EV + 1 + m2, ci + 2, li), sv(SV_EV + 1 + m2, ci + 3, li),
-                     sv(SV_EV + 1 + m2, ci + 4, li), sv(SV_EV + 1 + m2, ci + 5, li));
+    const T v1 = c2f(st.EV(1 + m1, ci + 2, li), st.EV(1 + m1, ci + 3, li), st.EV(1 + m1, ci + 4, li),
+                     st.EV(1 + m1, ci + 5, li));
+    const T v2 = c2f(st.EV(1 + m2, ci + 2, li), st.EV(1 + m2, ci + 3, li), st.EV(1 + m2, ci + 4, li),
+                     st.EV(1 + m2, ci + 5, li));
     b.M[(2 * D) * nc + c] = fi(c7(perm_row_c(D, T1)), ci + 1, li) + Bn * v1;
     b.M[(2 * D + 1) * nc + c] = fi(c7(perm_row_c(D, T2)), ci + 1, li) + Bn * v2;
   }
@@ -649,9 +804,9 @@ __global__ void __launch_bounds__(kThreads) k_emf(Bufs<T> b) {
   const T* Bz_fy = b.M + 3 * nc;
   const T* Bx_fz = b.M + 4 * nc;
   const T* By_fz = b.M + 5 * nc;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
-    int i, j, k;
-    decompose(c, n, &i, &j, &k);
+  int i, j, k;
+  long long c;
+  if (sweep_cell(n, &i, &j, &k, &c)) {
     auto I = [&](const T* f, int ax) {
       return c2f(f[nb(i, j, k, ax, -1, n)], f[c], f[nb(i, j, k, ax, 1, n)], f[nb(i, j, k, ax, 2, n)]);
     };
@@ -670,9 +825,9 @@ __global__ void __launch_bounds__(kThreads) k_emf_avg(Bufs<T> b) {
   FD_ACTIVE_OR_RETURN(b.ctl);
   const int n = b.a.n;
   const long long nc = b.a.nc;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
-    int i, j, k;
-    decompose(c, n, &i, &j, &k);
+  int i, j, k;
+  long long c;
+  if (sweep_cell(n, &i, &j, &k, &c)) {
     auto avg = [&](const T* q, int A, int B) {
       const T q0 = q[c];
       const T sx = (q[nb(i, j, k, A, -1, n)] - T(2) * q0 + q[nb(i, j, k, A, 1, n)]) / T(24);
@@ -754,9 +909,9 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
   const T* Oz = b.OB + 2 * nc;
   const int wlo = a.wind_lo, wn = a.wind ? a.wind_n : 0;
   const long long wn3 = (long long)wn * wn * wn;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
-    int i, j, k;
-    decompose(c, n, &i, &j, &k);
+  int i, j, k;
+  long long c;
+  if (sweep_cell(n, &i, &j, &k, &c)) {
     auto D6 = [&](const T* g, int ax) {
       return fd6(g[nb(i, j, k, ax, -3, n)], g[nb(i, j, k, ax, -2, n)], g[nb(i, j, k, ax, -1, n)], g[c],
                  g[nb(i, j, k, ax, 1, n)], g[nb(i, j, k, ax, 2, n)]);
@@ -774,8 +929,18 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
 #pragma unroll
       for (int r = 0; r < 5; ++r) ws[r] = b.WS[r * wn3 + w];
     }
+    // the flux differences summed in the reference's order, (x + y) + z
+    // (_ssprk.py:224-228); B_a's own-axis difference is exactly zero
     auto rhs = [&](int r) {
-      const T rq = -dtdx * b.ACC[r * nc + c];
+      const T* ax = b.ACC;
+      const T* ay = b.ACC + 8 * nc;
+      const T* az = b.ACC + 16 * nc;
+      T sum;
+      if (r == BX) sum = ay[r * nc + c] + az[r * nc + c];
+      else if (r == BY) sum = ax[r * nc + c] + az[r * nc + c];
+      else if (r == BZ) sum = ax[r * nc + c] + ay[r * nc + c];
+      else sum = (ax[r * nc + c] + ay[r * nc + c]) + az[r * nc + c];
+      const T rq = -dtdx * sum;
       return (wind && r < 5) ? rq + ws[r] : rq;
     };
     if (stage < 4) {
@@ -801,7 +966,7 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
   }
 }
 
-// q_final -> primitives, faces -> state; advances t (last block)
+// q_final -> primitives, faces -> state (k_advance then advances t)
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_finalize(Bufs<T> b) {
   FD_ACTIVE_OR_RETURN(b.ctl);
@@ -809,9 +974,9 @@ __global__ void __launch_bounds__(kThreads) k_finalize(Bufs<T> b) {
   const T gamma = T(a.gamma), rhomin = T(a.rhomin), pgmin = T(a.pgmin);
   const int n = a.n;
   const long long nc = a.nc;
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (long long)gridDim.x * blockDim.x) {
-    int i, j, k;
-    decompose(c, n, &i, &j, &k);
+  int i, j, k;
+  long long c;
+  if (sweep_cell(n, &i, &j, &k, &c)) {
     T U[8], P[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) U[r] = b.QF[r * nc + c];
@@ -823,18 +988,15 @@ __global__ void __launch_bounds__(kThreads) k_finalize(Bufs<T> b) {
 #pragma unroll
     for (int r = 0; r < 3; ++r) b.P[(8 + r) * nc + c] = b.BF[r * nc + c];
   }
-  __shared__ bool last;
-  if (threadIdx.x == 0) {
-    __threadfence();
-    last = (atomicAdd(&b.ctl->done_count, 1u) == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
+}
+
+// the step's time advance, after k_finalize (one thread)
+template <typename T>
+__global__ void k_advance(Bufs<T> b) {
+  FD_ACTIVE_OR_RETURN(b.ctl);
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
     b.ctl->t = b.ctl->t + b.ctl->dt;
     b.ctl->steps = b.ctl->steps + 1;
-    b.ctl->done_count = 0u;
-    __threadfence();
   }
 }
 
@@ -872,8 +1034,9 @@ int launch_stages(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t 
   constexpr int kA = WenoTile<T>::A, kL = WenoTile<T>::L, kWT = WenoTile<T>::THREADS;
   const dim3 wg((n + kA - 1) / kA, (n + kL - 1) / kL, n);
   const size_t wsm = weno_smem<T>();
+  const dim3 g3 = sweep_grid(n), b3 = sweep_block();
   for (int st = 0; st < 5; ++st) {
-    k_prep<T><<<g, kThreads, 0, s>>>(b, st);
+    k_prep<T><<<g3, b3, 0, s>>>(b, st);
     fd_mark(L, FD_PH_PREP, s);
     k_weno<T, 0><<<wg, kWT, wsm, s>>>(b);
     fd_mark(L, FD_PH_WENO_X, s);
@@ -881,9 +1044,9 @@ int launch_stages(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t 
     fd_mark(L, FD_PH_WENO_Y, s);
     k_weno<T, 2><<<wg, kWT, wsm, s>>>(b);
     fd_mark(L, FD_PH_WENO_Z, s);
-    k_emf<T><<<g, kThreads, 0, s>>>(b);
+    k_emf<T><<<g3, b3, 0, s>>>(b);
     fd_mark(L, FD_PH_EMF, s);
-    k_emf_avg<T><<<g, kThreads, 0, s>>>(b);
+    k_emf_avg<T><<<g3, b3, 0, s>>>(b);
     fd_mark(L, FD_PH_EMF_AVG, s);
     if (a.wind) {
       const long long wn3 = (long long)a.wind_n * a.wind_n * a.wind_n;
@@ -891,11 +1054,13 @@ int launch_stages(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t 
       k_wind_source<T><<<wg, kThreads, 0, s>>>(b, st);
       fd_mark(L, FD_PH_WIND, s);
     }
-    k_update<T><<<g, kThreads, 0, s>>>(b, st);
+    k_update<T><<<g3, b3, 0, s>>>(b, st);
     fd_mark(L, FD_PH_UPDATE, s);
   }
-  k_finalize<T><<<g, kThreads, 0, s>>>(b);
+  k_finalize<T><<<g3, b3, 0, s>>>(b);
   fd_mark(L, FD_PH_FINALIZE, s);
+  k_advance<T><<<1, 32, 0, s>>>(b);
+  fd_mark(L, FD_PH_ADVANCE, s);
   return cudaGetLastError() == cudaSuccess ? AMX_OK : AMX_ERR_CUDA;
 }
 

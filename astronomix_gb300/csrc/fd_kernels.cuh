@@ -72,15 +72,15 @@ struct FDArgs {
 // kernels of a step, for the per-kernel timing of amx_plan_profile
 enum FDPhase {
   FD_PH_CFL = 0, FD_PH_PREP, FD_PH_WENO_X, FD_PH_WENO_Y, FD_PH_WENO_Z, FD_PH_EMF, FD_PH_EMF_AVG, FD_PH_WIND,
-  FD_PH_UPDATE, FD_PH_FINALIZE, FD_PH_FORCING, FD_PH_COUNT
+  FD_PH_UPDATE, FD_PH_FINALIZE, FD_PH_FORCING, FD_PH_ADVANCE, FD_PH_COUNT
 };
-constexpr int kFDMaxMarks = 48;  // launches of one step (37, 42 with the wind source) + 1
+constexpr int kFDMaxMarks = 48;  // launches of one step (38, 43 with the wind source, 44 with forcing)
 
 // buffers and launch geometry handed from the host plan to the typed launchers
 struct FDLaunch {
   int grid;        // blocks of the pointwise sweeps
   int n;
-  void* bufs[10];  // Q0 Q QF QC ACC (8 rows) B BF (3) M (6) OM OB (3)
+  void* bufs[10];  // Q0 Q QF QC (8 rows) ACC (24) B BF (3) M (6) OM OB (3)
   FDControl* ctl;
   void* wind_src;  // stellar wind: [5][wind_n^3] source of the current stage (null without)
   // per-kernel timing (null when off): an event is recorded after every
@@ -471,7 +471,21 @@ __device__ __forceinline__ void R_col(const EigIF<T>& e, int s, T* R) {
   }
 }
 
-// WENO interpolant of _weno.py:190-205 / 213-228
+// Max for the WENO flux where a NaN operand needs no propagation of its own:
+// any NaN in a stencil cell already reaches the flux through the
+// projections, so the flux is NaN either way.  One min/max instruction in
+// FP32; the NaN-propagating jmax in FP64, whose arithmetic stays the
+// reference's.
+template <typename T>
+__device__ __forceinline__ T wmax(T a, T b) {
+  if constexpr (sizeof(T) == 4) return fmaxf(a, b);
+  else return jmax(a, b);
+}
+
+// WENO interpolant of _weno.py:190-205 / 213-228.  FP32: one reciprocal of
+// the weight sum and products with 1/3, 1/6 in place of four divisions (the
+// FP32 kernels are held to an L1 tolerance against FP64); FP64: the
+// reference's divisions.
 template <typename T>
 __device__ __forceinline__ T weno_phi(T a, T b, T c, T d) {
   const T eps = T(1e-8);
@@ -482,10 +496,15 @@ __device__ __forceinline__ T weno_phi(T a, T b, T c, T d) {
   const T al1 = T(6) / sq(eps + IS1);
   const T al2 = T(3) / sq(eps + IS2);
   T asum = al0 + al1 + al2;
-  asum = jmax(asum, T(1e-14));
-  const T w0 = al0 / asum;
-  const T w2 = al2 / asum;
-  return w0 * (a - T(2) * b + c) / T(3) + (w2 - T(0.5)) * (b - T(2) * c + d) / T(6);
+  asum = wmax(asum, T(1e-14));
+  if constexpr (sizeof(T) == 4) {
+    const T r = T(1) / asum;
+    return (al0 * r) * (a - T(2) * b + c) * T(1.0 / 3.0) + (al2 * r - T(0.5)) * (b - T(2) * c + d) * T(1.0 / 6.0);
+  } else {
+    const T w0 = al0 / asum;
+    const T w2 = al2 / asum;
+    return w0 * (a - T(2) * b + c) / T(3) + (w2 - T(0.5)) * (b - T(2) * c + d) / T(6);
+  }
 }
 
 // interp_center_to_face (_interpolate.py:9-21): (-f[-1] + 9 f[0] + 9 f[1] - f[2]) / 16

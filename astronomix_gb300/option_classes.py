@@ -13,8 +13,10 @@ integer constants:
 
 The config selects which CUDA kernel instantiation runs (solver, limiter,
 dimensionality, precision); the params are passed to the kernels as plain
-numbers.  Physics modules (wind, cooling, cosmic rays, learned forces,
-self-gravity, turbulent forcing) are outside the accelerated MHD step: their
+numbers.  Self-gravity (finite volume), turbulent forcing (3D) and the
+stellar-wind source of the finite-difference scheme run on the GPU with the
+step.  The other physics modules (cooling, cosmic rays, learned forces, the
+finite-volume wind injection) are outside the accelerated MHD step: their
 option classes exist so that configs built for astronomix still construct,
 and switching one on raises ``NotImplementedError`` in ``time_integration``.
 """

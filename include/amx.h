@@ -158,7 +158,7 @@ int amx_plan_set_limits(amx_plan* plan, int32_t max_fixed_point_iterations, int6
  * summed milliseconds and the launch counts since the last reset into
  * ms[n] / launches[n] (either may be null): 0 CFL, 1 stage prep, 2-4 WENO
  * x / y / z, 5 edge EMF, 6 EMF averages, 7 wind source, 8 stage update,
- * 9 finalize, 10 turbulent forcing.  AMX_ERR_UNSUPPORTED for an FV plan
+ * 9 finalize, 10 turbulent forcing, 11 time advance.  AMX_ERR_UNSUPPORTED for an FV plan
  * (one persistent launch per step). */
 int amx_plan_profile(amx_plan* plan, int32_t enable);
 int amx_plan_profile_read(amx_plan* plan, double* ms, int64_t* launches, int32_t n, int32_t reset);

@@ -4,9 +4,10 @@ Source: tests/mhd_tests/final_state_orszag_tang.npz of leo1200/astronomix
 0.5.1 (the FP64 final state of tests/mhd_tests/orszag_tang.py: 200^2 cells on
 [0, 2 pi]^2, HLL, MINMOD, C_cfl 0.4, t = 3).  The summary keeps the shape, the
 per-row sums, minima and maxima, and the density on every 8th cell in each
-direction, small enough to commit.  Run from the repository root:
+direction, small enough to commit.  Run from the repository root with the
+reference's source tree as the argument (or in AMX_REFERENCE_PATH):
 
-    python tests/golden/make_golden.py /path/to/astronomix
+    python tests/golden/make_golden.py /path/to/astronomix-checkout
 """
 import json
 import os
@@ -32,4 +33,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    path = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AMX_REFERENCE_PATH")
+    if not path:
+        sys.exit("usage: make_golden.py <reference source tree>")
+    main(path)
