@@ -83,6 +83,7 @@ amx::FVArgs<T> make_fv_args(amx_plan* p, void* state, const amx_params* prm, int
   a.limiter = c.limiter;
   a.integrator = c.fv_magnetic_integrator;
   a.lm = (c.riemann_solver == AMX_HLLC_LM);
+  a.am = (c.riemann_solver == AMX_AM_HLLC) ? 1 : (c.riemann_solver == AMX_HYBRID_HLLC ? 2 : 0);
   a.exact_end_time = c.exact_end_time;
   a.fixed_timestep = c.fixed_timestep;
   a.mode = mode;
@@ -249,7 +250,11 @@ int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out) 
   }
 
   // ---- FV kernel selection
-  const int rs = (cfg->riemann_solver == AMX_HLLC_LM) ? AMX_HLLC : cfg->riemann_solver;
+  // the HLLC family shares one kernel: HLLC-LM, HYBRID_HLLC and AM_HLLC are runtime modes of it
+  const int rs = (cfg->riemann_solver == AMX_HLLC_LM || cfg->riemann_solver == AMX_HYBRID_HLLC ||
+                  cfg->riemann_solver == AMX_AM_HLLC)
+                     ? AMX_HLLC
+                     : cfg->riemann_solver;
   const int scheme = cfg->split ? amx::FV_SPLIT
                                  : (cfg->limiter == AMX_VAN_ALBADA_PP ? amx::FV_UNSPLIT_PP : amx::FV_UNSPLIT);
   const bool ok = (cfg->dtype == AMX_F32)

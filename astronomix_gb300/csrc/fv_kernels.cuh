@@ -80,6 +80,7 @@ struct FVArgs {
   int limiter;
   int integrator;    // IMPLICIT_MIDPOINT / IMPLICIT_EULER
   int lm;            // HLLC-LM variant (riemann family HLLC)
+  int am;            // family HLLC: 1 AM_HLLC, 2 HYBRID_HLLC (HLLC-LM where the right cell is compressed), 0 none
   int exact_end_time;
   int fixed_timestep;
   int mode;
@@ -502,7 +503,14 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
           }
         }
         T F[NV];
-        riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), lm, F);
+        bool lmf = lm;
+        if (RS == RS_HLLC && a.am) {
+          // hll.py:268-326: the switch of the cell right of the face (the
+          // reference's flux index i is the face i - 1/2)
+          const int strides[3] = {G::H1 * G::H2, G::H2, 1};
+          lmf = am_compressed<T, DIM>(sP + h, G::HALO, strides, gamma, dxT);
+        }
+        riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), lmf, F, a.am == 1);
 #pragma unroll
         for (int v = 0; v < NV; ++v) sFk[v * fdim + f] = F[v];
       }
@@ -790,11 +798,12 @@ struct MagCtx {
   AxisMap<DIM> amap;
   __device__ __forceinline__ MagCtx(const FVArgs<T>& a, T* st)
       : state(st), nc(a.ncells), n(a.n), dx(T(a.dx)), midpoint(a.integrator == 0), amap(a) {}
-  // the cell `off` cells away along axis k, boundary-mapped
-  __device__ __forceinline__ long long neighbor(const int* ic, int k, int off) const {
+  // the cell `off` cells away along axis k, boundary-mapped; *flip is set
+  // when the cell is a reflective wall's mirror image
+  __device__ __forceinline__ long long neighbor(const int* ic, int k, int off, bool* flip) const {
     int j[3] = {ic[0], ic[1], ic[2]};
-    bool flip = false;
-    j[k] = amap(k, ic[k] + off, &flip);
+    *flip = false;
+    j[k] = amap(k, ic[k] + off, flip);
     return cell_index<DIM>(j[0], j[1], j[2], n);
   }
 };
@@ -813,10 +822,21 @@ __device__ __forceinline__ void mag_direct_cell(const MagCtx<T, DIM>& x, const M
   else { ic[2] = (int)(c % n); ic[1] = (int)((c / n) % n); ic[0] = (int)(c / ((long long)n * n)); }
   // averaged fields at the cell and its 2*DIM neighbours
   T Bc[3], vc[3], B0c[3], v0c[3];
-  auto avg_at = [&](long long cc, T* Ba, T* va, T* Bk_out, T* vk_out, T* B0_out, T* v0_out) {
+  // flip_c: the component of B and v that a reflective wall's ghost cell
+  // negates -- the reference fills the 3-vectors with
+  // _reflective_*_boundary(.., axis), which negates component `axis` (1
+  // for x, 2 for y) rather than the wall-normal one (boundaries.py:324-355,
+  // applied in _magnetic_field_update.py at every evaluation)
+  auto avg_at = [&](long long cc, T* Ba, T* va, T* Bk_out, T* vk_out, T* B0_out, T* v0_out, int flip_c = -1) {
     T Bk[3], vk[3], B0[3], v0[3];
     load_Bv<T, DIM>(src, cc, nc, Bk, vk);
     load_Bv<T, DIM>(s0, cc, nc, B0, v0);
+    if (flip_c >= 0) {
+      Bk[flip_c] = -Bk[flip_c];
+      vk[flip_c] = -vk[flip_c];
+      B0[flip_c] = -B0[flip_c];
+      v0[flip_c] = -v0[flip_c];
+    }
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       if (midpoint) { Ba[i] = (Bk[i] + B0[i]) / T(2); va[i] = (vk[i] + v0[i]) / T(2); }
@@ -831,11 +851,14 @@ __device__ __forceinline__ void mag_direct_cell(const MagCtx<T, DIM>& x, const M
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
     T Ba[3], va[3];
-    avg_at(x.neighbor(ic, k, +1), Ba, va, nullptr, nullptr, nullptr, nullptr);
+    bool fl;
+    const long long cp = x.neighbor(ic, k, +1, &fl);
+    avg_at(cp, Ba, va, nullptr, nullptr, nullptr, nullptr, (fl && k + 1 < 3) ? k + 1 : -1);
     cross3(Ba, va, Ep[k]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) Bp[k][i] = Ba[i];
-    avg_at(x.neighbor(ic, k, -1), Ba, va, nullptr, nullptr, nullptr, nullptr);
+    const long long cm = x.neighbor(ic, k, -1, &fl);
+    avg_at(cm, Ba, va, nullptr, nullptr, nullptr, nullptr, (fl && k + 1 < 3) ? k + 1 : -1);
     cross3(Ba, va, Em[k]);
 #pragma unroll
     for (int i = 0; i < 3; ++i) Bm[k][i] = Ba[i];

@@ -177,9 +177,12 @@ __device__ __forceinline__ void hll_flux(const T* qL, const T* qR, int d, T gamm
   for (int v = 0; v < NV; ++v) F[v] = (SR * FL[v] - SL * FR[v] + SLSR * (UR[v] - UL[v])) / den;
 }
 
-// HLLC and HLLC-LM (hll.py:123-261)
+// HLLC and HLLC-LM (hll.py:123-261); `lmdc`: the low-Mach dissipation
+// control of AM_HLLC (:230-254), the velocity rows of the dissipation scaled
+// by min(1, max |v| / c of the two states)
 template <typename T, int DIM>
-__device__ __forceinline__ void hllc_flux(const T* qL, const T* qR, int d, T gamma, bool lm, T* F) {
+__device__ __forceinline__ void hllc_flux(const T* qL, const T* qR, int d, T gamma, bool lm, T* F,
+                                          bool lmdc = false) {
   constexpr int NV = DIM + 2;
   const T rhoL = qL[0], rhoR = qR[0], pL = qL[NV - 1], pR = qR[NV - 1];
   const T uL = qL[d], uR = qR[d];
@@ -220,13 +223,36 @@ __device__ __forceinline__ void hllc_flux(const T* qL, const T* qR, int d, T gam
     SRs = SR * phi;
   }
   const T aS = Num<T>::abs_(S_star);
+  T fm = T(1);
+  if (lmdc) {
+    const T Ma = jmax(Num<T>::abs_(abs_velocity<T, DIM>(qL) / cL), Num<T>::abs_(abs_velocity<T, DIM>(qR) / cR));
+    fm = jmin(T(1), Ma);
+  }
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
-    const T Fs = T(0.5) * (FL[v] + FR[v]) +
-                 T(0.5) * (SLs * (USL[v] - UL[v]) + aS * (USL[v] - USR[v]) + SRs * (USR[v] - UR[v]));
+    T diss = T(0.5) * (SLs * (USL[v] - UL[v]) + aS * (USL[v] - USR[v]) + SRs * (USR[v] - UR[v]));
+    if (lmdc && v >= 1 && v <= DIM) diss = fm * diss;
+    const T Fs = T(0.5) * (FL[v] + FR[v]) + diss;
     T f = (SL >= T(0)) ? FL[v] : Fs;
     F[v] = (SR <= T(0)) ? FR[v] : f;
   }
+}
+
+// The compression switch of AM_HLLC / HYBRID_HLLC (hll.py:268-326) at a
+// cell of a primitive tile: div v by central differences (each axis
+// (v[+1] - v[-1]) / 2dx, summed in axis order) below -0.05 c / dx.
+// `q` points at the cell's density in a tile whose variable rows are
+// `vstride` apart; stride[a] is the cell stride along axis a.
+template <typename T, int DIM>
+__device__ __forceinline__ bool am_compressed(const T* q, int vstride, const int* stride, T gamma, T dx) {
+  T div = T(0);
+#pragma unroll
+  for (int a = 0; a < DIM; ++a) {
+    const T* v = q + (1 + a) * vstride;
+    div = div + (v[stride[a]] - v[-stride[a]]) / (T(2) * dx);
+  }
+  const T c = sound_speed(q[0], q[(DIM + 1) * vstride], gamma);
+  return div < T(-0.05) * c / dx;
 }
 
 // Lax-Friedrichs with the global alpha of the stage (_lax_friedrichs.py:21-78)
@@ -243,11 +269,13 @@ __device__ __forceinline__ void lf_flux(const T* qL, const T* qR, int d, T gamma
   for (int v = 0; v < NV; ++v) F[v] = T(0.5) * (FL[v] + FR[v]) - ha * (UR[v] - UL[v]);
 }
 
-// `lm` selects the HLLC-LM variant inside the HLLC family (runtime flag)
+// `lm` selects the HLLC-LM variant inside the HLLC family and `lmdc` the
+// low-Mach dissipation control (runtime flags)
 template <typename T, int DIM, int RS>
-__device__ __forceinline__ void riemann(const T* qL, const T* qR, int d, T gamma, T alpha, bool lm, T* F) {
+__device__ __forceinline__ void riemann(const T* qL, const T* qR, int d, T gamma, T alpha, bool lm, T* F,
+                                        bool lmdc = false) {
   if (RS == RS_HLL) hll_flux<T, DIM>(qL, qR, d, gamma, F);
-  else if (RS == RS_HLLC) hllc_flux<T, DIM>(qL, qR, d, gamma, lm, F);
+  else if (RS == RS_HLLC) hllc_flux<T, DIM>(qL, qR, d, gamma, lm, F, lmdc);
   else if (RS == RS_HLLC_LM) hllc_flux<T, DIM>(qL, qR, d, gamma, true, F);
   else lf_flux<T, DIM>(qL, qR, d, gamma, alpha, F);
 }

@@ -107,6 +107,7 @@ int launch(const amx_config* c, void* state, const amx_params* prm, int64_t max_
   a.limiter = c->limiter;
   a.integrator = c->fv_magnetic_integrator;
   a.lm = (c->riemann_solver == AMX_HLLC_LM);
+  a.am = (c->riemann_solver == AMX_AM_HLLC) ? 1 : (c->riemann_solver == AMX_HYBRID_HLLC ? 2 : 0);
   a.exact_end_time = c->exact_end_time;
   a.fixed_timestep = c->fixed_timestep;
   a.mode = amx::FV_MODE_STEPS;
@@ -171,7 +172,11 @@ extern "C" int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_
   if (rc) return rc;
 
   amx::FVKernelInfo kinfo{};
-  const int rs = (cfg->riemann_solver == AMX_HLLC_LM) ? AMX_HLLC : cfg->riemann_solver;
+  // the HLLC family shares one kernel: HLLC-LM, HYBRID_HLLC and AM_HLLC are runtime modes of it
+  const int rs = (cfg->riemann_solver == AMX_HLLC_LM || cfg->riemann_solver == AMX_HYBRID_HLLC ||
+                  cfg->riemann_solver == AMX_AM_HLLC)
+                     ? AMX_HLLC
+                     : cfg->riemann_solver;
   const int scheme = cfg->split ? amx::FV_SPLIT
                                  : (cfg->limiter == AMX_VAN_ALBADA_PP ? amx::FV_UNSPLIT_PP : amx::FV_UNSPLIT);
   const bool ok = (cfg->dtype == AMX_F32) ? amx::fv_kernel_f32(cfg->dimensionality, rs, cfg->mhd != 0, scheme, &kinfo)

@@ -49,6 +49,8 @@ extern "C" {
 #define AMX_HLLC 1
 #define AMX_HLLC_LM 2
 #define AMX_LAX_FRIEDRICHS 3
+#define AMX_HYBRID_HLLC 4  /* HLLC-LM where the cell right of a face is compressed, HLLC elsewhere (unsplit) */
+#define AMX_AM_HLLC 5      /* HYBRID_HLLC with the low-Mach dissipation control (unsplit) */
 
 #define AMX_MINMOD 0
 #define AMX_OSHER 1
@@ -83,7 +85,7 @@ typedef struct amx_config {
   int32_t num_cells;              /* cells per axis (square / cubic grids)      */
   int32_t num_vars;               /* rows of the state array                    */
   int32_t mhd;                    /* 0 / 1                                      */
-  int32_t riemann_solver;         /* AMX_HLL .. AMX_LAX_FRIEDRICHS              */
+  int32_t riemann_solver;         /* AMX_HLL .. AMX_AM_HLLC                     */
   int32_t limiter;                /* AMX_MINMOD .. AMX_VAN_ALBADA_PP            */
   int32_t fv_magnetic_integrator; /* AMX_IMPLICIT_MIDPOINT / _EULER             */
   int32_t numerical_precision;    /* 0: fixed-point tol 1e-5, 1: 1e-10          */

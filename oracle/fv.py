@@ -14,7 +14,7 @@ reference's ``axis`` argument) is array axis ``a``.
 from astronomix_gb300.option_classes import (
     GHOST_CELLS, OPEN_BOUNDARY, REFLECTIVE_BOUNDARY, PERIODIC_BOUNDARY,
     MINMOD, OSHER, DOUBLE_MINMOD, SUPERBEE, VAN_ALBADA, VAN_ALBADA_PP,
-    HLL, HLLC, HLLC_LM, LAX_FRIEDRICHS, UNSPLIT, RK2_SSP, MUSCL,
+    HLL, HLLC, HLLC_LM, LAX_FRIEDRICHS, HYBRID_HLLC, AM_HLLC, UNSPLIT, RK2_SSP, MUSCL,
     IMPLICIT_MIDPOINT, IMPLICIT_EULER, SINGLE_PRECISION, DOUBLE_PRECISION,
 )
 from ._xp import xp
@@ -422,8 +422,9 @@ def hll(PL, PR, gamma, dims, rv, d):
     return (SR * FL - SL * FR + SL * SR * (UR - UL)) / (SR - SL)
 
 
-def hllc(PL, PR, gamma, dims, rv, d, lm=False):
-    """_finite_volume/_riemann_solver/hll.py:123-261 (HLLC and HLLC-LM)."""
+def hllc(PL, PR, gamma, dims, rv, d, lm=False, lmdc=False):
+    """_finite_volume/_riemann_solver/hll.py:123-261 (HLLC and HLLC-LM;
+    `lmdc`: the low-Mach dissipation control of the velocity rows, :230-254)."""
     rhoL, uL, pL = PL[rv.density_index], PL[d], PL[rv.pressure_index]
     rhoR, uR, pR = PR[rv.density_index], PR[d], PR[rv.pressure_index]
     cL = speed_of_sound(rhoL, pL, gamma)
@@ -459,12 +460,37 @@ def hllc(PL, PR, gamma, dims, rv, d, lm=False):
         SRs = SR * phi
     else:
         SLs, SRs = SL, SR
-    F_star = 0.5 * (FL + FR) + 0.5 * (
-        SLs * (USL - UL) + xp.abs(S_star) * (USL - USR) + SRs * (USR - UR)
-    )
+    diss = 0.5 * (SLs * (USL - UL) + xp.abs(S_star) * (USL - USR) + SRs * (USR - UR))
+    if lmdc:
+        Ma = xp.maximum(xp.abs(get_absolute_velocity(PL, dims, rv) / cL),
+                        xp.abs(get_absolute_velocity(PR, dims, rv) / cR))
+        f = xp.minimum(1, Ma)
+        v0 = rv.velocity_index if dims == 1 else rv.velocity_index.x
+        diss = xp.copy(diss)
+        diss[v0:v0 + dims] = f * diss[v0:v0 + dims]
+    F_star = 0.5 * (FL + FR) + diss
     F = xp.where(SL >= 0, FL, F_star)
     F = xp.where(SR <= 0, FR, F)
     return F
+
+
+def am_hllc(PL, PR, P, gamma, config, rv, d):
+    """_finite_volume/_riemann_solver/hll.py:268-326: HLLC-LM where the cell
+    right of the interface is compressed (div v < -0.05 c / dx, central
+    differences of the stage state), HLLC elsewhere; AM_HLLC with the
+    low-Mach dissipation control, HYBRID_HLLC without."""
+    dims = config.dimensionality
+    dx = config.grid_spacing
+    a = speed_of_sound(P[rv.density_index], P[rv.pressure_index], gamma)
+    div_v = 0
+    for i in range(dims):
+        # _stencil_add(v_i, indices=(1, -1), factors=(1, -1), axis=i) / (2 dx)
+        div_v = div_v + (0 + 1.0 * xp.roll(P[i + 1], -1, i) + (-1.0) * xp.roll(P[i + 1], 1, i)) / (2 * dx)
+    g = xp.where(div_v < -0.05 * a / dx, 1, 0)
+    lmdc = config.riemann_solver == AM_HLLC
+    F_hllc = hllc(PL, PR, gamma, dims, rv, d, lm=False, lmdc=lmdc)
+    F_lm = hllc(PL, PR, gamma, dims, rv, d, lm=True, lmdc=lmdc)
+    return g * F_lm + (1 - g) * F_hllc
 
 
 def lax_friedrichs(PL, PR, P, gamma, dims, rv, d):
@@ -491,6 +517,8 @@ def riemann_solver(PL, PR, P, gamma, config, rv, d):
         return hllc(PL, PR, gamma, dims, rv, d, lm=True)
     if rs == LAX_FRIEDRICHS:
         return lax_friedrichs(PL, PR, P, gamma, dims, rv, d)
+    if rs in (AM_HLLC, HYBRID_HLLC):
+        return am_hllc(PL, PR, P, gamma, config, rv, d)
     raise NotImplementedError("Riemann solver %d is not part of the accelerated path" % rs)
 
 

@@ -30,10 +30,13 @@ def sod(n=101, dtype=np.float64, riemann=HLLC, limiter=MINMOD, t_end=0.2, C_cfl=
     return cfg, prm, rv, s
 
 
-def orszag_tang(n=64, dtype=np.float64, t_end=0.01, riemann=HLL, C_cfl=0.4, roll=False, limiter=MINMOD):
-    """2D Orszag-Tang vortex on [0,1]^2, gamma 5/3 (rho=25/(36 pi), p=5/(12 pi))."""
+def orszag_tang(n=64, dtype=np.float64, t_end=0.01, riemann=HLL, C_cfl=0.4, roll=False, limiter=MINMOD,
+                boundary=None):
+    """2D Orszag-Tang vortex on [0,1]^2, gamma 5/3 (rho=25/(36 pi), p=5/(12 pi));
+    `boundary`: one code for every side instead of periodic."""
+    bs = PERIODIC_2D if boundary is None else BoundarySettings(*[BoundarySettings1D(boundary, boundary)] * 3)
     cfg = SimulationConfig(mhd=True, dimensionality=2, box_size=1.0, num_cells=n, riemann_solver=riemann,
-                           limiter=limiter, boundary_settings=PERIODIC_2D,
+                           limiter=limiter, boundary_settings=bs,
                            boundary_handling=PERIODIC_ROLL if roll else 0)
     rv = get_registered_variables(cfg)
     dx = 1.0 / n

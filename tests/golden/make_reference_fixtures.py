@@ -95,7 +95,8 @@ def seam_cases(classes):
     import numpy as np
     import reference_cases as rc
     from astronomix_gb300 import (SimulationConfig, SimulationParams, finalize_config, get_registered_variables,
-                                  HLL, HLLC, HLLC_LM, LAX_FRIEDRICHS, MINMOD, OSHER, DOUBLE_MINMOD, SUPERBEE,
+                                  HLL, HLLC, HLLC_LM, LAX_FRIEDRICHS, AM_HLLC, HYBRID_HLLC, MINMOD, OSHER,
+                                  DOUBLE_MINMOD, SUPERBEE,
                                   VAN_ALBADA, PERIODIC_ROLL, FINITE_DIFFERENCE)
     from _cases import PERIODIC_2D
     from astronomix._finite_volume._riemann_solver._riemann_solver import _riemann_solver
@@ -131,7 +132,8 @@ def seam_cases(classes):
     out = {}
     PL, PR, P3 = rc.prim2d(1), rc.prim2d(2), rc.prim2d(3)
     for name, rs, d in (("riemann_hll", HLL, 1), ("riemann_hllc", HLLC, 2), ("riemann_hllc_lm", HLLC_LM, 1),
-                        ("riemann_lax_friedrichs", LAX_FRIEDRICHS, 1)):
+                        ("riemann_lax_friedrichs", LAX_FRIEDRICHS, 1), ("riemann_am_hllc", AM_HLLC, 1),
+                        ("riemann_hybrid_hllc", HYBRID_HLLC, 2)):
         cfg, rcfg, rrv = hydro2d(riemann=rs)
         out[name + "/output"] = np.asarray(_riemann_solver(PL, PR, P3, g, rcfg, rrv, d))
     P = rc.prim2d(4)

@@ -18,7 +18,7 @@ the cell-centre field refresh, one FD step.
 import numpy as np
 
 from astronomix_gb300 import (
-    HLL, HLLC, HLLC_LM, LAX_FRIEDRICHS, MINMOD, OSHER, DOUBLE_MINMOD, SUPERBEE, VAN_ALBADA, VAN_ALBADA_PP,
+    HLL, HLLC, HLLC_LM, LAX_FRIEDRICHS, HYBRID_HLLC, AM_HLLC, MINMOD, OSHER, DOUBLE_MINMOD, SUPERBEE, VAN_ALBADA, VAN_ALBADA_PP,
     OPEN_BOUNDARY, REFLECTIVE_BOUNDARY, PERIODIC_BOUNDARY, SPLIT, MUSCL, IMPLICIT_EULER,
 )
 
@@ -38,6 +38,14 @@ def _floored_blast(n=12):
 def _split(case):
     cfg, prm, rv, s = case
     return cfg._replace(split=SPLIT, time_integrator=MUSCL), prm, rv, s
+
+
+def _mixed():
+    """x reflective on the left and open on the right, y reflective on both sides."""
+    from astronomix_gb300 import BoundarySettings, BoundarySettings1D
+    return BoundarySettings(BoundarySettings1D(REFLECTIVE_BOUNDARY, OPEN_BOUNDARY),
+                            BoundarySettings1D(REFLECTIVE_BOUNDARY, REFLECTIVE_BOUNDARY),
+                            BoundarySettings1D(REFLECTIVE_BOUNDARY, REFLECTIVE_BOUNDARY))
 
 
 def _with(case, **kw):
@@ -70,6 +78,14 @@ RUN_CASES = {
     "mhd2d_van_albada_pp": lambda: smooth_random(2, 20, seed=19, mhd=True, limiter=VAN_ALBADA_PP, t_end=0.005),
     "mhd3d_hll": lambda: smooth_random(3, 12, seed=3, mhd=True, t_end=0.005),
     "mhd3d_lax_friedrichs": lambda: smooth_random(3, 12, seed=3, mhd=True, riemann=LAX_FRIEDRICHS, t_end=0.005),
+    "sod_am_hllc": lambda: sod(riemann=AM_HLLC, t_end=0.1),
+    "sod_hybrid_hllc": lambda: sod(riemann=HYBRID_HLLC, t_end=0.1),
+    "hydro2d_am_hllc": lambda: smooth_random(2, 24, seed=23, riemann=AM_HLLC, t_end=0.02, amp=0.5),
+    "hydro3d_hybrid_hllc": lambda: smooth_random(3, 12, seed=24, riemann=HYBRID_HLLC, t_end=0.02, amp=0.5),
+    "ot32_am_hllc": lambda: orszag_tang(n=32, t_end=0.02, riemann=AM_HLLC),
+    "ot32_reflective": lambda: orszag_tang(n=32, t_end=0.02, boundary=REFLECTIVE_BOUNDARY),
+    "mhd2d_reflective_open": lambda: _with(smooth_random(2, 24, seed=29, mhd=True, t_end=0.01,
+                                                         boundary=REFLECTIVE_BOUNDARY), boundary_settings=_mixed()),
     "fd_blast12_oblique": lambda: blast_fd(n=12, t_end=0.003, B=(0.6, 0.5, 0.4)),
     "fd_blast12_floors": lambda: _floored_blast(12),
     "fd_blast12_zero_normal_field": lambda: blast_fd(n=12, t_end=0.003),
@@ -127,6 +143,8 @@ SEAM_CASES = {
     "riemann_hllc": "HLLC, axis 2",
     "riemann_hllc_lm": "HLLC-LM, axis 1",
     "riemann_lax_friedrichs": "Lax-Friedrichs (global alpha over prim2d(3)), axis 1",
+    "riemann_am_hllc": "AM-HLLC (compression switch from prim2d(3)), axis 1",
+    "riemann_hybrid_hllc": "HYBRID_HLLC, axis 2",
     "limited_gradients": "limited gradients of prim2d(4) along axis 1 and 2 for every limiter",
     "magnetic_update_2d": "magnetic_update of mag2d(5), dt 1e-3, periodic roll",
     "cfl_fv_2d": "_cfl_time_step (UNSPLIT) of prim2d(6)",

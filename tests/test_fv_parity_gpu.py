@@ -193,3 +193,16 @@ def test_snapshot_magnetic_divergence_fp64(cuda):
         assert out.total_mass[i] == pytest.approx(q.total_mass, rel=1e-13)
         assert out.total_energy[i] == pytest.approx(q.total_energy, rel=1e-12)
     assert np.allclose(out.magnetic_divergence[:taken], out.magnetic_divergence[0], rtol=1e-10)
+
+
+@pytest.mark.parametrize("kw", [dict(riemann=5), dict(riemann=4), dict(boundary=REFLECTIVE_BOUNDARY)],
+                         ids=["am_hllc", "hybrid_hllc", "reflective_mhd"])
+def test_orszag_tang_variants_fp32_l1(cuda, kw):
+    """AM_HLLC / HYBRID_HLLC (hll.py:268-326) and reflective walls with MHD
+    (boundaries.py:324-355 on the B and v 3-vectors) in FP32 against the FP64
+    oracle; their FP64 runs are held to the reference's own results in
+    test_reference_fixtures_gpu.py."""
+    cfg, prm, rv, s = orszag_tang(n=32, t_end=0.02, dtype=np.float32, **kw)
+    got = amx.time_integration(s.copy(), cfg, prm, rv)
+    ref64 = odriver.time_integration(s.astype(np.float64), cfg, prm, rv)
+    assert rel_l1(got, ref64) < 1e-5

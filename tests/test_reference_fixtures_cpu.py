@@ -54,7 +54,8 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("name,rs,d", [("riemann_hll", 0, 1), ("riemann_hllc", 1, 2), ("riemann_hllc_lm", 2, 1),
-                                       ("riemann_lax_friedrichs", 3, 1)])
+                                       ("riemann_lax_friedrichs", 3, 1), ("riemann_am_hllc", 5, 1),
+                                       ("riemann_hybrid_hllc", 4, 2)])
 def test_oracle_riemann_solvers(name, rs, d):
     cfg, rv = _hydro2d(riemann=rs)
     got = ofv.riemann_solver(rc.prim2d(1), rc.prim2d(2), rc.prim2d(3), 5 / 3, cfg, rv, d)
