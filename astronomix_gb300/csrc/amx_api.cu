@@ -250,11 +250,7 @@ int amx_plan_create(const amx_config* cfg, int64_t max_history, amx_plan** out) 
   }
 
   // ---- FV kernel selection
-  // the HLLC family shares one kernel: HLLC-LM, HYBRID_HLLC and AM_HLLC are runtime modes of it
-  const int rs = (cfg->riemann_solver == AMX_HLLC_LM || cfg->riemann_solver == AMX_HYBRID_HLLC ||
-                  cfg->riemann_solver == AMX_AM_HLLC)
-                     ? AMX_HLLC
-                     : cfg->riemann_solver;
+  const int rs = amx::fv_riemann_family(cfg->riemann_solver);
   const int scheme = cfg->split ? amx::FV_SPLIT
                                  : (cfg->limiter == AMX_VAN_ALBADA_PP ? amx::FV_UNSPLIT_PP : amx::FV_UNSPLIT);
   const bool ok = (cfg->dtype == AMX_F32)

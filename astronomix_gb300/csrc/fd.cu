@@ -52,8 +52,8 @@ namespace {
 inline int ok(cudaError_t e) { return e == cudaSuccess ? AMX_OK : AMX_ERR_CUDA; }
 inline size_t a256(size_t x) { return (x + 255) & ~size_t(255); }
 
-// rows per buffer: Q0 Q QF QC ACC (x, y, z) B BF M OM OB
-const int kRows[10] = {8, 8, 8, 8, 24, 3, 3, 6, 3, 3};
+// rows per buffer: Q0 Q QF QC ACC (y, z) B BF M OM OB
+const int kRows[10] = {8, 8, 8, 8, 16, 3, 3, 6, 3, 3};
 
 fd::FDArgs make_args(const FDPlan* p, const amx_params& prm, double t_pause) {
   fd::FDArgs a;

@@ -56,7 +56,7 @@ struct Bufs {
   T* Q;    // 8
   T* QF;   // 8
   T* QC;   // 8
-  T* ACC;  // 3 x 8: the flux differences of the x, y and z interfaces
+  T* ACC;  // 2 x 8: the flux differences of the y and z interfaces (the x pass, last, sums them)
   T* B;    // 3  current face fields
   T* BF;   // 3  final accumulator of the faces
   T* M;    // 6  CT-corrected face fluxes: By_fx Bz_fx Bx_fy Bz_fy Bx_fz By_fz
@@ -618,11 +618,15 @@ __device__ __forceinline__ void weno_mode2(const EigIF<float>& e, const float2 (
 }
 
 // Interface fluxes along axis D (0 = x, 1 = y, 2 = z), _weno.py:112-324,
-// with the flux difference into acc and the CT-corrected fluxes of the two
-// tangential field components (_constrained_transport.py:77-102) fused into
-// the store.
+// with the CT-corrected fluxes of the two tangential field components
+// (_constrained_transport.py:77-102) fused into the store.  The z and y
+// passes run first and store their flux differences; the x pass, whose lanes
+// run along the contiguous z axis, adds its own to theirs and applies the
+// stage: the right-hand side of the cell-centred rows and the SSPRK(5,4)
+// combination (_ssprk.py:224-228, :298-310, :328-332).  The face fields are
+// k_update's, after the EMFs.
 template <typename T, int D>
-__global__ void __launch_bounds__(WenoTile<T>::THREADS, WenoTile<T>::BLOCKS) k_weno(Bufs<T> b) {
+__global__ void __launch_bounds__(WenoTile<T>::THREADS, WenoTile<T>::BLOCKS) k_weno(Bufs<T> b, int stage) {
   using W = WenoTile<T>;
   constexpr int kA = W::A, kL = W::L, kLP = W::LP, kAH = W::AH, kT = W::THREADS;
   FD_ACTIVE_OR_RETURN(b.ctl);
@@ -757,13 +761,20 @@ __global__ void __launch_bounds__(WenoTile<T>::THREADS, WenoTile<T>::BLOCKS) k_w
   }
   __syncthreads();
 
-  // ---- cells a0 .. a0+kA-1: the flux difference of this axis into its own
-  // buffer (a store, no read: the sum over axes is k_update's), the
-  // CT-corrected fluxes at their faces
+  // ---- cells a0 .. a0+kA-1: the flux difference of this axis (stored by
+  // the z and y passes; the x pass applies the stage), the CT-corrected
+  // fluxes at their faces
   // lab rows of the two tangential B components whose fluxes CT corrects
   constexpr int T1 = (D == 0) ? BY : BX;
   constexpr int T2 = (D == 2) ? BY : BZ;
-  T* const acc = b.ACC + (size_t)D * 8 * nc;
+  T* const acc = b.ACC + (size_t)(D == 0 ? 0 : D - 1) * 8 * nc;
+  // the x pass: stage constants and the stellar-wind cube
+  const T dt = (D == 0) ? T(*(volatile double*)&b.ctl->dt) : T(0);
+  const T dtdx = T(kRHS[stage]) * dt / T(a.dx);
+  const T k0 = T(kK0[stage]), kc = T(kKC[stage]);
+  const T fin = (stage < 4) ? T(kFIN[stage + 1]) : T(0);
+  const int wlo = a.wind_lo, wn = a.wind ? a.wind_n : 0;
+  const long long wn3 = (long long)wn * wn * wn;
   for (int task = threadIdx.x; task < kA * kL; task += kT) {
     int ci, li;
     if (D == 2) { ci = task % kA; li = task / kA; }
@@ -772,11 +783,59 @@ __global__ void __launch_bounds__(WenoTile<T>::THREADS, WenoTile<T>::BLOCKS) k_w
     if (ga >= n || gl >= n) continue;
     const long long c = cell_of(ga, gl);
     // face i+1/2 is local interface ci+1, face i-1/2 is ci
+    if constexpr (D != 0) {
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      const int k = c7(perm_row(D, r));
-      if (k < 0) continue;  // the flux of B along its own axis vanishes (k_update skips the row)
-      acc[r * nc + c] = fi(k, ci + 1, li) - fi(k, ci, li);
+      for (int r = 0; r < 8; ++r) {
+        const int k = c7(perm_row(D, r));
+        if (k < 0) continue;  // the flux of B along its own axis vanishes (never read)
+        acc[r * nc + c] = fi(k, ci + 1, li) - fi(k, ci, li);
+      }
+    } else {
+      // cell (i, j, k) = (ga, t3, gl); the wind source of this stage
+      // (k_wind_source) inside the taper's cube
+      T ws[5] = {T(0), T(0), T(0), T(0), T(0)};
+      const unsigned wi = (unsigned)(ga - wlo), wj = (unsigned)(t3 - wlo), wk = (unsigned)(gl - wlo);
+      const bool wind = wi < (unsigned)wn && wj < (unsigned)wn && wk < (unsigned)wn;
+      if (wind) {
+        const long long w = ((long long)wi * wn + wj) * wn + wk;
+#pragma unroll
+        for (int r = 0; r < 5; ++r) ws[r] = b.WS[r * wn3 + w];
+      }
+      // every load of the cell first (about 40 in flight per thread: the
+      // stores below may alias them for the compiler), then the arithmetic
+      const T* ay = b.ACC;
+      const T* az = b.ACC + 8 * nc;
+      T vy[8], vz[8], v0[8], vq[8], vf[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        // B_a's own-axis difference is exactly zero and never stored
+        vy[r] = (r != BY) ? ay[r * nc + c] : T(0);
+        vz[r] = (r != BZ) ? az[r * nc + c] : T(0);
+        vf[r] = b.QF[r * nc + c];
+        v0[r] = (stage < 4) ? b.Q0[r * nc + c] : T(0);
+        vq[r] = (stage < 4) ? b.Q[r * nc + c] : T(0);
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        // the flux differences summed in the reference's order, (x + y) + z
+        T sum;
+        if (r == BX) sum = vy[r] + vz[r];
+        else {
+          const T ax = fi(c7(r), ci + 1, li) - fi(c7(r), ci, li);
+          if (r == BY) sum = ax + vz[r];
+          else if (r == BZ) sum = ax + vy[r];
+          else sum = (ax + vy[r]) + vz[r];
+        }
+        const T rq0 = -dtdx * sum;
+        const T rq = (wind && r < 5) ? rq0 + ws[r] : rq0;
+        if (stage < 4) {
+          const T q = k0 * v0[r] + kc * vq[r] + rq;
+          b.Q[r * nc + c] = q;
+          b.QF[r * nc + c] = vf[r] + q * fin;
+        } else {
+          b.QF[r * nc + c] = vf[r] + rq;
+        }
+      }
     }
     // c2f over cells i-1 .. i+2 (staged rows ci+2 .. ci+5) of B_d and v_t (lab frame)
     const T Bn = c2f(st.U(BX, ci + 2, li), st.U(BX, ci + 3, li), st.U(BX, ci + 4, li), st.U(BX, ci + 5, li));
@@ -890,7 +949,9 @@ __global__ void __launch_bounds__(kThreads) k_wind_source(Bufs<T> b, int stage) 
   }
 }
 
-// RHS and the SSPRK(5,4) combination (_ssprk.py:224-228, :298-310, :328-332)
+// The face fields' right-hand side (the EMF curl) and their SSPRK(5,4)
+// combination (_ssprk.py:224-228, :298-310, :328-332); the cell-centred rows
+// are the x WENO pass's
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
   FD_ACTIVE_OR_RETURN(b.ctl);
@@ -907,8 +968,6 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
   const T* Ox = b.OB;
   const T* Oy = b.OB + nc;
   const T* Oz = b.OB + 2 * nc;
-  const int wlo = a.wind_lo, wn = a.wind ? a.wind_n : 0;
-  const long long wn3 = (long long)wn * wn * wn;
   int i, j, k;
   long long c;
   if (sweep_cell(n, &i, &j, &k, &c)) {
@@ -920,37 +979,7 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
     rb[0] = -dtdx * D6(Oz, 1) + dtdx * D6(Oy, 2);
     rb[1] = -dtdx * D6(Ox, 2) + dtdx * D6(Oz, 0);
     rb[2] = -dtdx * D6(Oy, 0) + dtdx * D6(Ox, 1);
-    // the wind source of this stage (k_wind_source), for the cells of the taper's cube
-    T ws[5] = {T(0), T(0), T(0), T(0), T(0)};
-    const unsigned wi = (unsigned)(i - wlo), wj = (unsigned)(j - wlo), wk = (unsigned)(k - wlo);
-    const bool wind = wi < (unsigned)wn && wj < (unsigned)wn && wk < (unsigned)wn;
-    if (wind) {
-      const long long w = ((long long)wi * wn + wj) * wn + wk;
-#pragma unroll
-      for (int r = 0; r < 5; ++r) ws[r] = b.WS[r * wn3 + w];
-    }
-    // the flux differences summed in the reference's order, (x + y) + z
-    // (_ssprk.py:224-228); B_a's own-axis difference is exactly zero
-    auto rhs = [&](int r) {
-      const T* ax = b.ACC;
-      const T* ay = b.ACC + 8 * nc;
-      const T* az = b.ACC + 16 * nc;
-      T sum;
-      if (r == BX) sum = ay[r * nc + c] + az[r * nc + c];
-      else if (r == BY) sum = ax[r * nc + c] + az[r * nc + c];
-      else if (r == BZ) sum = ax[r * nc + c] + ay[r * nc + c];
-      else sum = (ax[r * nc + c] + ay[r * nc + c]) + az[r * nc + c];
-      const T rq = -dtdx * sum;
-      return (wind && r < 5) ? rq + ws[r] : rq;
-    };
     if (stage < 4) {
-#pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        const T rq = rhs(r);
-        const T q = k0 * b.Q0[r * nc + c] + kc * b.Q[r * nc + c] + rq;
-        b.Q[r * nc + c] = q;
-        b.QF[r * nc + c] = b.QF[r * nc + c] + q * f;
-      }
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
         const T bn = k0 * b0[r * nc + c] + kc * bcur[r * nc + c] + rb[r];
@@ -958,8 +987,6 @@ __global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
         b.BF[r * nc + c] = b.BF[r * nc + c] + bn * f;
       }
     } else {
-#pragma unroll
-      for (int r = 0; r < 8; ++r) b.QF[r * nc + c] = b.QF[r * nc + c] + rhs(r);
 #pragma unroll
       for (int r = 0; r < 3; ++r) b.BF[r * nc + c] = b.BF[r * nc + c] + rb[r];
     }
@@ -1038,22 +1065,23 @@ int launch_stages(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t 
   for (int st = 0; st < 5; ++st) {
     k_prep<T><<<g3, b3, 0, s>>>(b, st);
     fd_mark(L, FD_PH_PREP, s);
-    k_weno<T, 0><<<wg, kWT, wsm, s>>>(b);
-    fd_mark(L, FD_PH_WENO_X, s);
-    k_weno<T, 1><<<wg, kWT, wsm, s>>>(b);
-    fd_mark(L, FD_PH_WENO_Y, s);
-    k_weno<T, 2><<<wg, kWT, wsm, s>>>(b);
-    fd_mark(L, FD_PH_WENO_Z, s);
-    k_emf<T><<<g3, b3, 0, s>>>(b);
-    fd_mark(L, FD_PH_EMF, s);
-    k_emf_avg<T><<<g3, b3, 0, s>>>(b);
-    fd_mark(L, FD_PH_EMF_AVG, s);
-    if (a.wind) {
+    if (a.wind) {  // from the stage's input (QC); the x pass adds it
       const long long wn3 = (long long)a.wind_n * a.wind_n * a.wind_n;
       const int wg = (int)((wn3 + kThreads - 1) / kThreads < g ? (wn3 + kThreads - 1) / kThreads : g);
       k_wind_source<T><<<wg, kThreads, 0, s>>>(b, st);
       fd_mark(L, FD_PH_WIND, s);
     }
+    // z and y store their flux differences; x (last) applies the stage to Q
+    k_weno<T, 2><<<wg, kWT, wsm, s>>>(b, st);
+    fd_mark(L, FD_PH_WENO_Z, s);
+    k_weno<T, 1><<<wg, kWT, wsm, s>>>(b, st);
+    fd_mark(L, FD_PH_WENO_Y, s);
+    k_weno<T, 0><<<wg, kWT, wsm, s>>>(b, st);
+    fd_mark(L, FD_PH_WENO_X, s);
+    k_emf<T><<<g3, b3, 0, s>>>(b);
+    fd_mark(L, FD_PH_EMF, s);
+    k_emf_avg<T><<<g3, b3, 0, s>>>(b);
+    fd_mark(L, FD_PH_EMF_AVG, s);
     k_update<T><<<g3, b3, 0, s>>>(b, st);
     fd_mark(L, FD_PH_UPDATE, s);
   }

@@ -80,7 +80,7 @@ constexpr int kFDMaxMarks = 48;  // launches of one step (38, 43 with the wind s
 struct FDLaunch {
   int grid;        // blocks of the pointwise sweeps
   int n;
-  void* bufs[10];  // Q0 Q QF QC (8 rows) ACC (24) B BF (3) M (6) OM OB (3)
+  void* bufs[10];  // Q0 Q QF QC (8 rows) ACC (16) B BF (3) M (6) OM OB (3)
   FDControl* ctl;
   void* wind_src;  // stellar wind: [5][wind_n^3] source of the current stage (null without)
   // per-kernel timing (null when off): an event is recorded after every

@@ -41,6 +41,10 @@ bool fv_kernel_f32_schemes(int dim, int rs, bool mhd, int scheme, FVKernelInfo* 
   AMX_FV_SCHEME_CASE(3, RS_HLL, true, FV_UNSPLIT_PP)
   AMX_FV_SCHEME_CASE(3, RS_HLLC, true, FV_UNSPLIT_PP)
   AMX_FV_SCHEME_CASE(3, RS_LF, true, FV_UNSPLIT_PP)
+  AMX_FV_SCHEME_CASE(2, RS_AM, false, FV_UNSPLIT_PP)
+  AMX_FV_SCHEME_CASE(2, RS_AM, true, FV_UNSPLIT_PP)
+  AMX_FV_SCHEME_CASE(3, RS_AM, false, FV_UNSPLIT_PP)
+  AMX_FV_SCHEME_CASE(3, RS_AM, true, FV_UNSPLIT_PP)
   return false;
 }
 

@@ -29,6 +29,12 @@ bool fv_kernel_f64(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out) {
   AMX_FV_CASE(3, RS_HLL, true)
   AMX_FV_CASE(3, RS_HLLC, true)
   AMX_FV_CASE(3, RS_LF, true)
+  // AM_HLLC / HYBRID_HLLC (unsplit only)
+  AMX_FV_CASE(1, RS_AM, false)
+  AMX_FV_CASE(2, RS_AM, false)
+  AMX_FV_CASE(2, RS_AM, true)
+  AMX_FV_CASE(3, RS_AM, false)
+  AMX_FV_CASE(3, RS_AM, true)
   return false;
 }
 

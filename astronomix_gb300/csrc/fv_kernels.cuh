@@ -504,7 +504,7 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
         }
         T F[NV];
         bool lmf = lm;
-        if (RS == RS_HLLC && a.am) {
+        if constexpr (RS == RS_AM) {
           // hll.py:268-326: the switch of the cell right of the face (the
           // reference's flux index i is the face i - 1/2)
           const int strides[3] = {G::H1 * G::H2, G::H2, 1};
@@ -831,11 +831,13 @@ __device__ __forceinline__ void mag_direct_cell(const MagCtx<T, DIM>& x, const M
     T Bk[3], vk[3], B0[3], v0[3];
     load_Bv<T, DIM>(src, cc, nc, Bk, vk);
     load_Bv<T, DIM>(s0, cc, nc, B0, v0);
-    if (flip_c >= 0) {
-      Bk[flip_c] = -Bk[flip_c];
-      vk[flip_c] = -vk[flip_c];
-      B0[flip_c] = -B0[flip_c];
-      v0[flip_c] = -v0[flip_c];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const T sg = (i == flip_c) ? T(-1) : T(1);  // exact
+      Bk[i] *= sg;
+      vk[i] *= sg;
+      B0[i] *= sg;
+      v0[i] *= sg;
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -1082,11 +1084,12 @@ __device__ __forceinline__ void mag_finalize_cell(const T* state, T* out, long l
 
 // The work items of the FV step as the single-run and the batched kernels
 // call them: one hydro tile, and a strided range of cells of the fixed-point
-// map or of the write-back.  In FP64 they are separate (not inlined)
-// functions, so both kernels execute the same compiled arithmetic: IEEE
-// division leaves branches in the code around which the compiler may fuse
-// multiply-adds differently in different callers.  In FP32 (approximate
-// division, straight-line code) inlining already gives identical results.
+// map or of the write-back.  Where they are separate (not inlined)
+// functions, every kernel executes the same compiled arithmetic: branches
+// (IEEE division, data-dependent selects) let the compiler fuse
+// multiply-adds differently in different callers.  The FP32 hydro tile
+// (approximate division, straight-line code) is inlined and gives identical
+// results all the same.
 template <typename T, int DIM, int RS, int V>
 struct FVItems {
   template <bool PP = false>
@@ -1106,39 +1109,22 @@ struct FVItems<double, DIM, RS, V> {
   }
 };
 
+// The magnetic items are separate functions in both precisions: the
+// reflective walls' sign flips put data-dependent selects into the map.
 template <typename T, int DIM>
 struct MagItems {
-  static __device__ __forceinline__ void direct(const FVArgs<T>& a, T* state, const MagSrc<T, DIM>& src, T* dst,
-                                                T dt, long long c, long long end, long long step, T* change) {
+  static __device__ __noinline__ void direct(const FVArgs<T>& a, T* state, const MagSrc<T, DIM>& src, T* dst, T dt,
+                                             long long c, long long end, long long step, T* change) {
     const MagCtx<T, DIM> x(a, state);
     T ch = *change;
     for (; c < end; c += step) mag_direct_cell<T, DIM>(x, src, dst, dt, c, ch);
     *change = ch;
   }
-  static __device__ __forceinline__ void finalize(const FVArgs<T>& a, const T* state, const T* Bv, T* out,
-                                                  long long c, long long end, long long step, bool track,
-                                                  T* m) {
+  static __device__ __noinline__ void finalize(const FVArgs<T>& a, const T* state, const T* Bv, T* out, long long c,
+                                               long long end, long long step, bool track, T* m) {
     const long long nc = a.ncells;
     const T gamma = T(a.gamma);
     for (; c < end; c += step) mag_finalize_cell<T, DIM>(state, out, nc, gamma, Bv, c, track, m);
-  }
-};
-template <int DIM>
-struct MagItems<double, DIM> {
-  static __device__ __noinline__ void direct(const FVArgs<double>& a, double* state, const MagSrc<double, DIM>& src,
-                                             double* dst, double dt, long long c, long long end, long long step,
-                                             double* change) {
-    const MagCtx<double, DIM> x(a, state);
-    double ch = *change;
-    for (; c < end; c += step) mag_direct_cell<double, DIM>(x, src, dst, dt, c, ch);
-    *change = ch;
-  }
-  static __device__ __noinline__ void finalize(const FVArgs<double>& a, const double* state, const double* Bv,
-                                               double* out, long long c, long long end, long long step, bool track,
-                                               double* m) {
-    const long long nc = a.ncells;
-    const double gamma = a.gamma;
-    for (; c < end; c += step) mag_finalize_cell<double, DIM>(state, out, nc, gamma, Bv, c, track, m);
   }
 };
 

@@ -155,7 +155,10 @@ __device__ __forceinline__ T limited(T bd, T fd, int limiter, T dx) {
 
 // ------------------------------------------------------------ Riemann solvers
 
-enum { RS_HLL = 0, RS_HLLC = 1, RS_HLLC_LM = 2, RS_LF = 3 };
+// RS_AM: the HLLC family with the compression switch of AM_HLLC /
+// HYBRID_HLLC (FVArgs::am), a kernel of its own so that plain HLLC carries
+// none of its code
+enum { RS_HLL = 0, RS_HLLC = 1, RS_HLLC_LM = 2, RS_LF = 3, RS_AM = 4 };
 
 // HLL (hll.py:36-109)
 template <typename T, int DIM>
@@ -230,9 +233,13 @@ __device__ __forceinline__ void hllc_flux(const T* qL, const T* qR, int d, T gam
   }
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
-    T diss = T(0.5) * (SLs * (USL[v] - UL[v]) + aS * (USL[v] - USR[v]) + SRs * (USR[v] - UR[v]));
-    if (lmdc && v >= 1 && v <= DIM) diss = fm * diss;
-    const T Fs = T(0.5) * (FL[v] + FR[v]) + diss;
+    T Fs;
+    if (lmdc && v >= 1 && v <= DIM)
+      Fs = T(0.5) * (FL[v] + FR[v]) +
+           fm * (T(0.5) * (SLs * (USL[v] - UL[v]) + aS * (USL[v] - USR[v]) + SRs * (USR[v] - UR[v])));
+    else
+      Fs = T(0.5) * (FL[v] + FR[v]) +
+           T(0.5) * (SLs * (USL[v] - UL[v]) + aS * (USL[v] - USR[v]) + SRs * (USR[v] - UR[v]));
     T f = (SL >= T(0)) ? FL[v] : Fs;
     F[v] = (SR <= T(0)) ? FR[v] : f;
   }
@@ -275,7 +282,8 @@ template <typename T, int DIM, int RS>
 __device__ __forceinline__ void riemann(const T* qL, const T* qR, int d, T gamma, T alpha, bool lm, T* F,
                                         bool lmdc = false) {
   if (RS == RS_HLL) hll_flux<T, DIM>(qL, qR, d, gamma, F);
-  else if (RS == RS_HLLC) hllc_flux<T, DIM>(qL, qR, d, gamma, lm, F, lmdc);
+  else if (RS == RS_HLLC) hllc_flux<T, DIM>(qL, qR, d, gamma, lm, F);
+  else if (RS == RS_AM) hllc_flux<T, DIM>(qL, qR, d, gamma, lm, F, lmdc);
   else if (RS == RS_HLLC_LM) hllc_flux<T, DIM>(qL, qR, d, gamma, true, F);
   else lf_flux<T, DIM>(qL, qR, d, gamma, alpha, F);
 }

@@ -10,7 +10,8 @@ struct FVKernelInfo {
   size_t smem_pp;      // extra shared memory with the VAN_ALBADA_PP limiter
 };
 
-// riemann family: 0 = HLL, 1 = HLLC (and HLLC-LM), 3 = Lax-Friedrichs
+// riemann family: 0 = HLL, 1 = HLLC (and HLLC-LM), 3 = Lax-Friedrichs,
+// 4 = HLLC with the AM_HLLC / HYBRID_HLLC compression switch (fv_riemann_family)
 // scheme: FV_UNSPLIT, FV_SPLIT or FV_UNSPLIT_PP (fv_kernels.cuh)
 bool fv_kernel_f32(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out);
 bool fv_kernel_f64(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out);

@@ -172,11 +172,7 @@ extern "C" int amx_fv_run_noalloc(const amx_config* cfg, void* state, const amx_
   if (rc) return rc;
 
   amx::FVKernelInfo kinfo{};
-  // the HLLC family shares one kernel: HLLC-LM, HYBRID_HLLC and AM_HLLC are runtime modes of it
-  const int rs = (cfg->riemann_solver == AMX_HLLC_LM || cfg->riemann_solver == AMX_HYBRID_HLLC ||
-                  cfg->riemann_solver == AMX_AM_HLLC)
-                     ? AMX_HLLC
-                     : cfg->riemann_solver;
+  const int rs = amx::fv_riemann_family(cfg->riemann_solver);
   const int scheme = cfg->split ? amx::FV_SPLIT
                                  : (cfg->limiter == AMX_VAN_ALBADA_PP ? amx::FV_UNSPLIT_PP : amx::FV_UNSPLIT);
   const bool ok = (cfg->dtype == AMX_F32) ? amx::fv_kernel_f32(cfg->dimensionality, rs, cfg->mhd != 0, scheme, &kinfo)

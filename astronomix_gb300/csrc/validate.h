@@ -8,6 +8,15 @@
 
 namespace amx {
 
+// The FV kernel family of a Riemann solver: HLLC-LM is a runtime mode of the
+// HLLC kernel; AM_HLLC and HYBRID_HLLC share a kernel (4) whose compression
+// switch is a runtime mode (FVArgs::am).
+inline int fv_riemann_family(int riemann_solver) {
+  if (riemann_solver == AMX_HLLC_LM) return AMX_HLLC;
+  if (riemann_solver == AMX_HYBRID_HLLC || riemann_solver == AMX_AM_HLLC) return 4;
+  return riemann_solver;
+}
+
 inline int validate_config(const amx_config* c) {
   if (!c) return AMX_ERR_INVALID_ARG;
   if (c->dtype != AMX_F32 && c->dtype != AMX_F64) return AMX_ERR_INVALID_ARG;
