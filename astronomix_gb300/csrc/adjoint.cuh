@@ -138,14 +138,14 @@ __device__ __forceinline__ void hll_vjp(const T* qL, const T* qR, int d, T gamma
   const T a1 = uL + cL, a2 = uR + cR, b1 = uL - cL, b2 = uR - cR;
   const T ma = jmax(a1, a2), mb = jmin(b1, b2);
   const T SR = jmax(ma, T(0)), SL = jmin(mb, T(0));
-  const T den = SR - SL;
+  const T rden = T(1) / (SR - SL);
   T lnum[NV], lFL[NV], lFR[NV], lUL[NV], lUR[NV];
   T lden = T(0), lSR = T(0), lSL = T(0);
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
     const T num = SR * FL[v] - SL * FR[v] + SL * SR * (UR[v] - UL[v]);
-    lnum[v] = lF[v] / den;
-    lden -= lF[v] * (num / den) / den;
+    lnum[v] = lF[v] * rden;
+    lden -= lnum[v] * num * rden;
     lFL[v] = SR * lnum[v];
     lFR[v] = -SL * lnum[v];
     lUR[v] = SL * SR * lnum[v];
@@ -163,11 +163,12 @@ __device__ __forceinline__ void hll_vjp(const T* qL, const T* qR, int d, T gamma
   lqL[d] += la1 + lb1;
   lqR[d] += la2 + lb2;
   // c = sqrt(gamma p / rho)
-  const T kL = lcL * T(0.5) / cL * gamma / rhoL, kR = lcR * T(0.5) / cR * gamma / rhoR;
+  const T rrL = T(1) / rhoL, rrR = T(1) / rhoR;
+  const T kL = lcL * (T(0.5) * gamma) * rrL / cL, kR = lcR * (T(0.5) * gamma) * rrR / cR;
   lqL[E] += kL;
-  lqL[0] -= kL * pL / rhoL;
+  lqL[0] -= kL * pL * rrL;
   lqR[E] += kR;
-  lqR[0] -= kR * pR / rhoR;
+  lqR[0] -= kR * pR * rrR;
   euler_flux_vjp<T, DIM>(qL, d, gamma, lFL, lqL);
   euler_flux_vjp<T, DIM>(qR, d, gamma, lFR, lqR);
   prim_to_cons_vjp<T, DIM>(qL, lUL, gamma, lqL);
@@ -201,6 +202,11 @@ __device__ __forceinline__ long long shifted(const int* ic, int k, int off, int 
 // Line tiles of the flux adjoint along axis K: L = 32 cells along K by W = 8
 // lines along J (the contiguous axis when K is not, else the next-to-last
 // axis); the halo of a line costs 3 + 3 cells of 32.
+//
+// Shared memory per line: P (PL cells), lU and the limited slope D
+// (UL cells each), the cotangents of qL and qR (FL faces each) and, in FP32,
+// the two partial derivatives of the limiter (UL cells each); FP64 recomputes
+// those in the cell phase so that two blocks still fit on an SM.
 template <int DIM, int K>
 struct AxisTile {
   static constexpr bool KFAST = (K == DIM - 1);
@@ -213,8 +219,10 @@ struct AxisTile {
   // a single round
   static constexpr int THREADS = W * (L + 4);
   template <typename T>
+  static constexpr bool keep_partials() { return sizeof(T) == 4; }
+  template <typename T>
   static constexpr size_t smem(int nv) {
-    return sizeof(T) * (size_t)nv * W * (PL + UL + 2 * FL);
+    return sizeof(T) * (size_t)nv * W * (PL + 2 * UL + 2 * FL + (keep_partials<T>() ? 2 * UL : 0));
   }
 };
 
@@ -234,16 +242,20 @@ struct AxisTile {
 // sets (or, with `accumulate`, adds) lPin = (d cons(P_in))^T lU + its own
 // flux terms.  The other passes add their flux terms to lPin.
 template <typename T, int DIM, int K, bool FIRST>
-__global__ void __launch_bounds__(AxisTile<DIM, K>::THREADS, sizeof(T) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(AxisTile<DIM, K>::THREADS, sizeof(T) == 4 ? 3 : 2)
 k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lPout, T* lU, T* lPin, T* lP0,
              int accumulate, T h) {
   using A = AxisTile<DIM, K>;
   constexpr int NV = DIM + 2, L = A::L, W = A::W;
+  constexpr bool KEEP = A::template keep_partials<T>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* sP = reinterpret_cast<T*>(smem_raw);   // [NV][W][PL], cell m at m + 3
   T* sU = sP + NV * W * A::PL;              // [NV][W][UL], cell m at m + 2
-  T* sLL = sU + NV * W * A::UL;             // [NV][W][FL] cotangent of qL, face f at f + 1
+  T* sD = sU + NV * W * A::UL;              // [NV][W][UL] limited slope, cell m at m + 2
+  T* sLL = sD + NV * W * A::UL;             // [NV][W][FL] cotangent of qL, face f at f + 1
   T* sLR = sLL + NV * W * A::FL;
+  T* sGa = sLR + NV * W * A::FL;            // [NV][W][UL] d minmod / d backward difference (FP32)
+  T* sGb = sGa + NV * W * A::UL;            // d minmod / d forward difference
   const int n = g.n;
   const long long nc = g.nc;
   const T gamma = T(g.gamma);
@@ -260,8 +272,11 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
   const int oK = bK * L, oJ = bJ * W, oM = (DIM == 3) ? (int)b : 0;
 
   auto cell = [&](int l, int w) -> long long {  // l may be outside [0, L): periodic along K
+    int x = oK + l;
+    while (x < 0) x += n;
+    while (x >= n) x -= n;
     int ic[3] = {0, 0, 0};
-    ic[K] = ((oK + l) % n + n) % n;
+    ic[K] = x;
     ic[A::J] = oJ + w;
     if (DIM == 3) ic[A::M] = oM;
     return cell_index<DIM>(ic[0], ic[1], ic[2], n);
@@ -307,14 +322,28 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
     for (int v = 0; v < NV; ++v) sU[(v * W + w) * A::UL + m + 2] = lu[v];
   }
   __syncthreads();
-  // the limited slope D[m] of the line at cell m and its partial derivatives
-  // (recomputed where needed: cheaper than shared-memory round trips)
-  auto slope = [&](const T* sp, int m, T* ga, T* gb) -> T {
-    const T bd = (sp[m] - sp[m - 1]) / dxT, fd = (sp[m + 1] - sp[m]) / dxT;
-    if (ga) minmod_d(bd, fd, ga, gb);
-    return limited(bd, fd, 0, dxT) * dxT / T(2);
-  };
-  // faces f in [-1, L+1]
+  // the limited slope D[m] = minmod(bd, fd) dx / 2 of every cell m in
+  // [-2, L+1], once (and in FP32 its partial derivatives)
+  for (int e = threadIdx.x; e < W * A::UL; e += blockDim.x) {
+    int w, m;
+    split(e, A::UL, &w, &m);
+    if (oJ + w >= n) continue;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const T* sp = sP + (v * W + w) * A::PL + 1;  // cell m at sp[m]
+      const T bd = (sp[m] - sp[m - 1]) / dxT, fd = (sp[m + 1] - sp[m]) / dxT;
+      const int o = (v * W + w) * A::UL + m;
+      sD[o] = limited(bd, fd, 0, dxT) * dxT / T(2);
+      if (KEEP) {
+        T ga, gb;
+        minmod_d(bd, fd, &ga, &gb);
+        sGa[o] = ga;
+        sGb[o] = gb;
+      }
+    }
+  }
+  __syncthreads();
+  // faces f in [-1, L+1]: qL = P[f-1] + D[f-1], qR = P[f] - D[f]
   for (int e = threadIdx.x; e < W * A::FL; e += blockDim.x) {
     int w, f;
     split(e, A::FL, &w, &f);
@@ -324,8 +353,9 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       const T* sp = sP + (v * W + w) * A::PL + 3;
-      qL[v] = sp[f - 1] + slope(sp, f - 1, nullptr, nullptr);
-      qR[v] = sp[f] - slope(sp, f, nullptr, nullptr);
+      const T* d = sD + (v * W + w) * A::UL + 2;
+      qL[v] = sp[f - 1] + d[f - 1];
+      qR[v] = sp[f] - d[f];
       const T* u = sU + (v * W + w) * A::UL + 2;
       // U[i] += inv_dx (F[i-1/2] - F[i+1/2]) h: face f feeds cell f (+) and f - 1 (-)
       lF[v] = inv_dx * (u[f] - u[f - 1]) * h;
@@ -351,11 +381,20 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
     for (int v = 0; v < NV; ++v) {
       const T* LL = sLL + (v * W + w) * A::FL + 1;
       const T* LR = sLR + (v * W + w) * A::FL + 1;
-      const T* sp = sP + (v * W + w) * A::PL + 3;
-      T ga0, gb0, gap, gbp, gam, gbm;
-      slope(sp, l, &ga0, &gb0);
-      slope(sp, l + 1, &gap, &gbp);
-      slope(sp, l - 1, &gam, &gbm);
+      T ga0, gb0, gap, gbm;
+      if (KEEP) {
+        const int o = (v * W + w) * A::UL + 2 + l;
+        ga0 = sGa[o];
+        gb0 = sGb[o];
+        gap = sGa[o + 1];
+        gbm = sGb[o - 1];
+      } else {
+        const T* sp = sP + (v * W + w) * A::PL + 3;
+        T t0, t1;
+        minmod_d((sp[l] - sp[l - 1]) / dxT, (sp[l + 1] - sp[l]) / dxT, &ga0, &gb0);
+        minmod_d((sp[l + 1] - sp[l]) / dxT, (sp[l + 2] - sp[l + 1]) / dxT, &gap, &t0);
+        minmod_d((sp[l - 1] - sp[l - 2]) / dxT, (sp[l] - sp[l - 1]) / dxT, &t1, &gbm);
+      }
       // cotangent of the slope D[m] = lqL[m+1] - lqR[m]
       const T dm1 = LL[l] - LR[l - 1], d0 = LL[l + 1] - LR[l], dp1 = LL[l + 2] - LR[l + 1];
       r[v] = LL[l + 1] + LR[l] + d0 * (ga0 - gb0) / T(2) - dp1 * gap / T(2) + dm1 * gbm / T(2);
@@ -655,9 +694,9 @@ k_tape_mag(FVArgs<T> a, const T* Z, T* Zn, T h) {
 
 template <typename T, int DIM>
 __global__ void __launch_bounds__(kFVThreads)
-k_tape_final(FVArgs<T> a, const T* Z) {
+k_tape_final(FVArgs<T> a, const T* Z, T* out) {
   T m[3] = {T(0), T(0), T(0)};
-  MagItems<T, DIM>::finalize(a, a.state, Z, a.state, (long long)blockIdx.x * blockDim.x + threadIdx.x, a.ncells,
+  MagItems<T, DIM>::finalize(a, a.state, Z, out, (long long)blockIdx.x * blockDim.x + threadIdx.x, a.ncells,
                              (long long)gridDim.x * blockDim.x, false, m);
 }
 
@@ -742,7 +781,6 @@ int tape_step(FVArgs<T> a, const StepTape<T>& t, bool mhd, cudaStream_t s) {
   using G = TileGeom<T, DIM>;
   constexpr int NVG = DIM + 2;
   const long long nc = a.ncells;
-  const int nvt = NVG + (mhd ? 3 : 0);
   const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
   const unsigned tiles = (unsigned)ntiles;
   const T dtT = T(t.dt);
@@ -759,10 +797,8 @@ int tape_step(FVArgs<T> a, const StepTape<T>& t, bool mhd, cudaStream_t s) {
   const int gb = grid_for(nc);
   for (int j = 0; j <= t.iters; ++j)
     k_tape_mag<T, DIM><<<gb, kFVThreads, 0, s>>>(am, j ? t.Z + 6 * (j - 1) * nc : nullptr, t.Z + 6 * j * nc, dtT);
-  if (cudaMemcpyAsync(t.S3, S2, sizeof(T) * nvt * nc, cudaMemcpyDeviceToDevice, s)) return AMX_ERR_CUDA;
-  FVArgs<T> af = a;
-  af.state = t.S3;
-  k_tape_final<T, DIM><<<gb, kFVThreads, 0, s>>>(af, t.Z + 6 * t.iters * nc);
+  // the write-back S3 = W(S2, Z_k), out of place (every row of S3 written)
+  k_tape_final<T, DIM><<<gb, kFVThreads, 0, s>>>(am, t.Z + 6 * t.iters * nc, t.S3);
   k_tape_stage<T, DIM><<<tiles, kFVThreads, G::SMEM, s>>>(a, t.S3, t.S4, nullptr, h);
   if (cudaMemcpyAsync(t.S5 + NVG * nc, t.S3 + NVG * nc, sizeof(T) * 3 * nc, cudaMemcpyDeviceToDevice, s))
     return AMX_ERR_CUDA;
