@@ -871,7 +871,8 @@ def run_ours(args, rank, world):
         tf = flop_per_cell * n ** 3 / weno_s / 1e12
         compute = {"achieved": tf, "peak": fp32_peak, "unit": "TFLOP/s", "frac": tf / fp32_peak,
                    "flop_per_cell_per_launch": flop_per_cell,
-                   "note": "FP32 flops counted by ncu (fadd + fmul + 2 ffma) per k_weno launch / cells; "
+                   "note": "FP32 flops counted by ncu per k_weno launch / cells: fadd + fmul + 2 ffma + "
+                           "2 (fadd2 + fmul2 + 2 ffma2), the paired instructions doing two operations; "
                            "peak = amx_probe_fp32_fma (register-only FMA chains on every SM)"}
 
     # ---- end to end through the C ABI with host buffers (pinned)
