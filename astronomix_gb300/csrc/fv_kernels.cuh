@@ -227,11 +227,17 @@ template <int DIM>
 struct AxisMap {
   int n;
   bool roll;
+  bool reflective;  // some wall of the first DIM axes mirrors (and flips a velocity)
   AxisBC bc[3];
   template <typename T>
   __device__ __forceinline__ explicit AxisMap(const FVArgs<T>& a) : n(a.n), roll(a.periodic_roll != 0) {
+    reflective = false;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) bc[k] = a.bc[k];
+    for (int k = 0; k < 3; ++k) {
+      bc[k] = a.bc[k];
+      if (k < DIM && (bc[k].lo == AMX_BC_REFLECTIVE || bc[k].hi == AMX_BC_REFLECTIVE)) reflective = true;
+    }
+    if (roll) reflective = false;
   }
   __device__ __forceinline__ int operator()(int k, int g, bool* flip) const {
     if (g < -2) g = -2;
@@ -393,20 +399,52 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
   T* sD = sF + NV * G::FMAX;           // [NV][SMAX] slopes (already * dx / 2)
 
   // ---- load the halo'd tile of primitives (boundary-mapped)
-  for (int e = threadIdx.x; e < G::HALO; e += blockDim.x) {
-    const int h2 = e % G::H2;
-    const int h1 = (e / G::H2) % G::H1;
-    const int h0 = e / (G::H2 * G::H1);
-    bool f0 = false, f1 = false, f2 = false;
-    const int i0 = amap(0, o[0] + h0 - 2, &f0);
-    const int i1 = (DIM >= 2) ? amap(1, o[1] + h1 - 2, &f1) : 0;
-    const int i2 = (DIM >= 3) ? amap(2, o[2] + h2 - 2, &f2) : 0;
-    const long long c = cell_index<DIM>(i0, i1, i2, n);
+  if constexpr (DIM == 3) {
+    // 3D (4.5 halo cells per tile cell, HBM-bound): every thread issues all
+    // of its copies (cp.async) before waiting for any; a reflective wall's
+    // sign flips are applied afterwards by the thread that copied the cell
+    for (int e = threadIdx.x; e < G::HALO; e += blockDim.x) {
+      const int h2 = e % G::H2;
+      const int h1 = (e / G::H2) % G::H1;
+      const int h0 = e / (G::H2 * G::H1);
+      bool f = false;
+      const long long c =
+          cell_index<DIM>(amap(0, o[0] + h0 - 2, &f), amap(1, o[1] + h1 - 2, &f), amap(2, o[2] + h2 - 2, &f), n);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      T val = Pin[v * nc + c];
-      if ((v == 1 && f0) || (v == 2 && f1) || (v == 3 && f2)) val = -val;
-      sP[v * G::HALO + e] = val;
+      for (int v = 0; v < NV; ++v) cp_async_elem(sP + v * G::HALO + e, Pin + v * nc + c);
+    }
+    cp_async_commit();
+    cp_async_wait_all();
+    if (amap.reflective) {
+      for (int e = threadIdx.x; e < G::HALO; e += blockDim.x) {
+        const int h2 = e % G::H2;
+        const int h1 = (e / G::H2) % G::H1;
+        const int h0 = e / (G::H2 * G::H1);
+        bool f0 = false, f1 = false, f2 = false;
+        amap(0, o[0] + h0 - 2, &f0);
+        amap(1, o[1] + h1 - 2, &f1);
+        amap(2, o[2] + h2 - 2, &f2);
+        if (f0) sP[1 * G::HALO + e] = -sP[1 * G::HALO + e];
+        if (f1) sP[2 * G::HALO + e] = -sP[2 * G::HALO + e];
+        if (f2) sP[3 * G::HALO + e] = -sP[3 * G::HALO + e];
+      }
+    }
+  } else {
+    for (int e = threadIdx.x; e < G::HALO; e += blockDim.x) {
+      const int h2 = e % G::H2;
+      const int h1 = (e / G::H2) % G::H1;
+      const int h0 = e / (G::H2 * G::H1);
+      bool f0 = false, f1 = false, f2 = false;
+      const int i0 = amap(0, o[0] + h0 - 2, &f0);
+      const int i1 = (DIM >= 2) ? amap(1, o[1] + h1 - 2, &f1) : 0;
+      const int i2 = (DIM >= 3) ? amap(2, o[2] + h2 - 2, &f2) : 0;
+      const long long c = cell_index<DIM>(i0, i1, i2, n);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        T val = Pin[v * nc + c];
+        if ((v == 1 && f0) || (v == 2 && f1) || (v == 3 && f2)) val = -val;
+        sP[v * G::HALO + e] = val;
+      }
     }
   }
   __syncthreads();
@@ -456,7 +494,7 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
         for (int v = 0; v < NV; ++v) {
           const T* s = sP + v * G::HALO + h;
           const T qm = s[-stride], q0 = s[0], qp = s[stride];
-          sDk[v * sdim + e] = limited((q0 - qm) / dxT, (qp - q0) / dxT, limiter, dxT) * dxT / T(2);
+          sDk[v * sdim + e] = half_slope(qm, q0, qp, limiter, dxT);
         }
       }
     }
@@ -496,10 +534,8 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
             qR[v] = s[0] - d[0];
           } else {
             const T qm2 = s[-2 * stride], qm1 = s[-stride], q0 = s[0], qp1 = s[stride];
-            const T gm1 = limited((qm1 - qm2) / dxT, (q0 - qm1) / dxT, limiter, dxT);
-            const T g0 = limited((q0 - qm1) / dxT, (qp1 - q0) / dxT, limiter, dxT);
-            qL[v] = qm1 + gm1 * dxT / T(2);
-            qR[v] = q0 - g0 * dxT / T(2);
+            qL[v] = qm1 + half_slope(qm2, qm1, q0, limiter, dxT);
+            qR[v] = q0 - half_slope(qm1, q0, qp1, limiter, dxT);
           }
         }
         T F[NV];
@@ -951,6 +987,7 @@ __device__ __forceinline__ void mag_tile(const FVArgs<T>& a, const T* state, con
   const long long nc = a.ncells;
   const int n = a.n;
   const T dx = T(a.dx);
+  const T hdx = T(0.5 * a.inv_dx);
   const bool midpoint = (a.integrator == 0);
   const AxisMap<DIM> amap(a);
   T* sB = smem;                 // [3][MHALO] averaged B
@@ -982,9 +1019,12 @@ __device__ __forceinline__ void mag_tile(const FVArgs<T>& a, const T* state, con
     const long long c = cell_index<DIM>(g0, g1, g2, n);
     const int h = ((c0 + 1) * G::M1 + (c1 + 1)) * G::M2 + (DIM >= 3 ? c2 + 1 : 0);
     const int st[3] = {G::M1 * G::M2, G::M2, 1};
-    // d(F_i)/d(x_k) = 0.5 (F_i[+] - F_i[-]) / dx  (_vector_maths.py:55-100)
+    // d(F_i)/d(x_k) = 0.5 (F_i[+] - F_i[-]) / dx  (_vector_maths.py:55-100);
+    // FP32 multiplies by 0.5 / dx instead of dividing
     auto dF = [&](const T* F, int i, int k) {
-      return T(0.5) * (F[i * G::MHALO + h + st[k]] - F[i * G::MHALO + h - st[k]]) / dx;
+      const T d = F[i * G::MHALO + h + st[k]] - F[i * G::MHALO + h - st[k]];
+      if constexpr (sizeof(T) == 4) return d * hdx;
+      else return T(0.5) * d / dx;
     };
     T curlE[3], curlB[3];
     if (DIM == 2) {
@@ -1199,12 +1239,13 @@ fv_run_kernel(FVArgs<T> a) {
   auto stage = [&](const T* in, T* out, const T* p0, T h, bool need) -> bool {
     set_alpha();
     unsigned long long* slot = produce_slot();
-    if constexpr (pp)
+    if constexpr (pp) {
       phase_hydro_stage<T, DIM, RS, true>(a, in, out, p0, h, RS == RS_LF ? s_alpha : nullptr, smem, slot, red,
                                           s_ppC);
-    else
+    } else {
       phase_hydro_stage<T, DIM, RS>(a, in, out, p0, h, RS == RS_LF ? s_alpha : nullptr, smem,
                                     (need || RS == RS_LF) ? slot : nullptr, red);
+    }
     ++rp;
     return grid_sync(bar, status);
   };

@@ -131,6 +131,22 @@ template <typename T> __device__ __forceinline__ T minmod3(T a, T b, T c) {
   return same ? sgn(a) * jmin(Num<T>::abs_(a), jmin(Num<T>::abs_(b), Num<T>::abs_(c))) : T(0);
 }
 
+// minmod(a, b) by cases: the smaller magnitude when a and b share a sign,
+// else 0 -- equal to the sign formula for every finite input (a NaN gives 0
+// here; the cell's own NaN still reaches its interface states)
+template <typename T> __device__ __forceinline__ T minmod_cases(T a, T b) {
+  return (a > T(0) && b > T(0)) ? (b < a ? b : a) : ((a < T(0) && b < T(0)) ? (b > a ? b : a) : T(0));
+}
+
+// The limited slope times dx / 2 of a cell from its neighbours, as the
+// reconstruction adds it to the interface states: the reference's
+// limited((q0 - qm) / dx, (qp - q0) / dx) dx / 2 (limited_gradients.py:22-88,
+// reconstruction.py:399-431).  FP32 with MINMOD takes minmod(q0 - qm,
+// qp - q0) / 2 directly: the same value up to the rounding of the two
+// divisions and the product by dx, with no division.
+template <typename T>
+__device__ __forceinline__ T half_slope(T qm, T q0, T qp, int limiter, T dx);
+
 // limited gradient from the backward/forward differences (already / dx)
 template <typename T>
 __device__ __forceinline__ T limited(T bd, T fd, int limiter, T dx) {
@@ -151,6 +167,14 @@ __device__ __forceinline__ T limited(T bd, T fd, int limiter, T dx) {
       return ((fd * fd + eps) * bd + (bd * bd + eps) * fd) / (fd * fd + bd * bd + T(2) * eps);
     }
   }
+}
+
+template <typename T>
+__device__ __forceinline__ T half_slope(T qm, T q0, T qp, int limiter, T dx) {
+  if constexpr (sizeof(T) == 4) {
+    if (limiter == 0) return minmod_cases(q0 - qm, qp - q0) * T(0.5);
+  }
+  return limited((q0 - qm) / dx, (qp - q0) / dx, limiter, dx) * dx / T(2);
 }
 
 // ------------------------------------------------------------ Riemann solvers

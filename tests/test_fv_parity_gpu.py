@@ -77,6 +77,26 @@ def test_hydro_2d_nonperiodic_fp64(cuda, boundary):
     assert rel_err(got, ref) < FP64_TOL
 
 
+@pytest.mark.parametrize("boundary", [OPEN_BOUNDARY, REFLECTIVE_BOUNDARY])
+def test_hydro_3d_nonperiodic_fp64(cuda, boundary):
+    """The 3D stage runs as per-axis line passes, each mapping its own
+    axis's boundary (a reflective wall negates that axis's velocity)."""
+    cfg, prm, rv, s = smooth_random(3, 10, seed=8, boundary=boundary, t_end=0.01)
+    got, ref, rec = run_both(cfg, prm, rv, s)
+    assert rec["steps"] >= 2
+    assert rel_err(got, ref) < FP64_TOL
+
+
+@pytest.mark.parametrize("riemann", [HLLC, LAX_FRIEDRICHS])
+def test_hydro_3d_partial_line_tiles_fp64(cuda, riemann):
+    """36 cells per axis: a full 32-cell line tile and a partial one along
+    every axis, and (FP64) partial lane blocks."""
+    cfg, prm, rv, s = smooth_random(3, 36, seed=9, riemann=riemann, t_end=0.003)
+    got, ref, rec = run_both(cfg, prm, rv, s)
+    assert rec["steps"] >= 2
+    assert rel_err(got, ref) < FP64_TOL
+
+
 @pytest.mark.parametrize("roll", [False, True])
 @pytest.mark.parametrize("riemann", [HLL, HLLC])
 def test_orszag_tang_fp64(cuda, roll, riemann):
