@@ -48,6 +48,14 @@ __device__ __forceinline__ bool sweep_cell(int n, int* i, int* j, int* k, long l
   *c = cidx(*i, *j, *k, n);
   return true;
 }
+// Resident blocks per SM that the FP32 prep and EMF sweeps budget their
+// registers for (AMX_FD_SWEEP_BLOCKS; latency-bound sweeps: more warps in
+// flight).  256^3 ms per launch, prep / EMF / EMF average: 0.33 / 0.17 /
+// 0.13 at the compiler's own budget, 0.31 / 0.15 / 0.12 at 6 blocks,
+// 0.30 / 0.18 / 0.12 at 8 (spills in the EMF sweeps).
+#ifndef AMX_FD_SWEEP_BLOCKS
+#define AMX_FD_SWEEP_BLOCKS 6
+#endif
 // The EMF sweeps, whose stencils reach along x: a thread takes XW
 // consecutive x cells of one (y, z) column, loads each x plane of an
 // x-direction stencil once, and has XW cells' loads in flight.  (The face
@@ -178,7 +186,7 @@ __device__ __forceinline__ void ucc(T* U, const T* bx, const T* by, const T* bz,
 // stage prep: positivity of q (stages 0-3) and the cell-centre refresh qc.
 // Stage 0 also forms q0 = cons(P) and the initial final-accumulators.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_prep(Bufs<T> b, int stage) {
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? AMX_FD_SWEEP_BLOCKS : 1) k_prep(Bufs<T> b, int stage) {
   FD_ACTIVE_OR_RETURN(b.ctl);
   const FDArgs a = b.a;
   const T gamma = T(a.gamma), rhomin = T(a.rhomin), pgmin = T(a.pgmin);
@@ -239,19 +247,21 @@ __host__ __device__ constexpr int c7(int row) { return row < BX ? row : (row == 
 
 // Tile of A cells along the flux axis x 32 lanes across it.  Every staged
 // cell (A + 6 with the halo of 3) costs a flux and an eigensystem; every
-// thread owns whole interfaces.  Shared memory is a structure of arrays
-// with a row pitch of 33 values, so that a warp reading 32 lanes of one row
-// (the interface sweep) and a warp reading 32 cells of one lane (the
-// staging and the store of the z-axis tile) are both free of bank
-// conflicts.  FP32: A = 11, 128 threads (the 12 x 32 interfaces are three
-// per thread), three blocks per SM (168 registers a thread, 63 KB of shared
-// memory a block), so that one block's staging loads and stores overlap the
-// others' arithmetic.  Measured on the 256^3 blast, WENO x / y / z ms per
-// launch: 1.50 / 1.49 / 1.60 (11, 128, 3 blocks), 1.53 / 1.51 / 1.56 (23,
-// 192, 2), 1.64 / 1.63 / 1.69 (47, 384, 1).  FP64: A = 15, 256 threads,
-// one block.
+// thread owns whole interfaces.  FP32: 128 threads, three blocks per SM (168
+// registers a thread, 62-70 KB of shared memory a block), so that one
+// block's staging loads and stores overlap the others' arithmetic; A = 13
+// for the y and z passes, 11 for the x pass, whose stage epilogue reads 40
+// values a cell.  Measured on the 256^3 blast, WENO x / y / z ms per launch
+// (bank-conflict-free layout): 1.71 / 1.40 / 1.42 with A = 11, 1.77 / 1.36 /
+// 1.38 with A = 13, 1.94 / 1.48 / 1.50 with A = 9; with the earlier layout
+// 1.50 / 1.49 / 1.60 (11, 128 threads, 3 blocks, before the x pass took the
+// stage), 1.53 / 1.51 / 1.56 (23, 192, 2), 1.64 / 1.63 / 1.69 (47, 384, 1).
+// FP64: A = 15, 256 threads, one block.
 #ifndef AMX_WENO_A32
 #define AMX_WENO_A32 11
+#endif
+#ifndef AMX_WENO_A32_YZ
+#define AMX_WENO_A32_YZ 13
 #endif
 #ifndef AMX_WENO_T32
 #define AMX_WENO_T32 128
@@ -259,8 +269,8 @@ __host__ __device__ constexpr int c7(int row) { return row < BX ? row : (row == 
 #ifndef AMX_WENO_B32
 #define AMX_WENO_B32 3
 #endif
-template <typename T> struct WenoTile {
-  static constexpr int A = sizeof(T) == 4 ? AMX_WENO_A32 : 15;
+template <typename T, int D> struct WenoTile {
+  static constexpr int A = sizeof(T) == 4 ? (D == 0 ? AMX_WENO_A32 : AMX_WENO_A32_YZ) : 15;
   static constexpr int THREADS = sizeof(T) == 4 ? AMX_WENO_T32 : 256;
   static constexpr int BLOCKS = sizeof(T) == 4 ? AMX_WENO_B32 : 1;  // resident blocks per SM
   static constexpr int L = 32;
@@ -277,9 +287,9 @@ template <typename T> struct WenoTile {
 // with an odd pitch along the axis: warps that step across lanes (the
 // interface sweep, the x and y staging) and warps that step along the axis
 // (the z staging) both hit 32 distinct banks, for 4- and 8-byte values.
-template <typename T>
+template <typename T, int D>
 constexpr size_t weno_smem() {
-  using W = WenoTile<T>;
+  using W = WenoTile<T, D>;
   return sizeof(T) * ((size_t)kSV * W::L * W::AH + (size_t)7 * W::L * W::FP);
 }
 constexpr int kSX = 9;  // FP32 scalar rows: 0 Bx, 1-5 eigenvector-block inputs, 6-8 cf ca cs
@@ -648,8 +658,8 @@ __device__ __forceinline__ void weno_mode2(const EigIF<float>& e, const float2 (
 // combination (_ssprk.py:224-228, :298-310, :328-332).  The face fields are
 // k_update's, after the EMFs.
 template <typename T, int D>
-__global__ void __launch_bounds__(WenoTile<T>::THREADS, WenoTile<T>::BLOCKS) k_weno(Bufs<T> b, int stage) {
-  using W = WenoTile<T>;
+__global__ void __launch_bounds__(WenoTile<T, D>::THREADS, WenoTile<T, D>::BLOCKS) k_weno(Bufs<T> b, int stage) {
+  using W = WenoTile<T, D>;
   constexpr int kA = W::A, kL = W::L, kFP = W::FP, kAH = W::AH, kT = W::THREADS;
   FD_ACTIVE_OR_RETURN(b.ctl);
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -875,7 +885,7 @@ __global__ void __launch_bounds__(WenoTile<T>::THREADS, WenoTile<T>::BLOCKS) k_w
 
 // edge EMFs (_constrained_transport.py:104-131)
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_emf(Bufs<T> b) {
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? AMX_FD_SWEEP_BLOCKS : 1) k_emf(Bufs<T> b) {
   FD_ACTIVE_OR_RETURN(b.ctl);
   const int n = b.a.n;
   const long long nc = b.a.nc;
@@ -916,7 +926,7 @@ __global__ void __launch_bounds__(kThreads) k_emf(Bufs<T> b) {
 
 // point values -> averages (_interpolate.py:39-62)
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_emf_avg(Bufs<T> b) {
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? AMX_FD_SWEEP_BLOCKS : 1) k_emf_avg(Bufs<T> b) {
   FD_ACTIVE_OR_RETURN(b.ctl);
   const int n = b.a.n;
   const long long nc = b.a.nc;
@@ -1001,9 +1011,15 @@ __global__ void __launch_bounds__(kThreads) k_wind_source(Bufs<T> b, int stage) 
 
 // The face fields' right-hand side (the EMF curl) and their SSPRK(5,4)
 // combination (_ssprk.py:224-228, :298-310, :328-332); the cell-centred rows
-// are the x WENO pass's
+// are the x WENO pass's.  Latency-bound (24 stencil loads a cell): in FP32
+// the register budget is set for AMX_FD_UPDATE_BLOCKS resident blocks per SM
+// (8: 32 registers, 0.53 -> 0.39 ms per 256^3 launch against the compiler's
+// own 48 registers).
+#ifndef AMX_FD_UPDATE_BLOCKS
+#define AMX_FD_UPDATE_BLOCKS 8
+#endif
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_update(Bufs<T> b, int stage) {
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? AMX_FD_UPDATE_BLOCKS : 1) k_update(Bufs<T> b, int stage) {
   FD_ACTIVE_OR_RETURN(b.ctl);
   const FDArgs a = b.a;
   const int n = a.n;
@@ -1095,10 +1111,12 @@ Bufs<T> make_bufs(const FDLaunch& L, void* state, const FDArgs& a) {
 
 template <typename T>
 int set_attrs() {
-  const int smem = (int)weno_smem<T>();
-  int rc = cudaFuncSetAttribute(k_weno<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess;
-  rc |= cudaFuncSetAttribute(k_weno<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess;
-  rc |= cudaFuncSetAttribute(k_weno<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess;
+  int rc = cudaFuncSetAttribute(k_weno<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)weno_smem<T, 0>()) !=
+           cudaSuccess;
+  rc |= cudaFuncSetAttribute(k_weno<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)weno_smem<T, 1>()) !=
+        cudaSuccess;
+  rc |= cudaFuncSetAttribute(k_weno<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)weno_smem<T, 2>()) !=
+        cudaSuccess;
   return rc ? AMX_ERR_CUDA : AMX_OK;
 }
 
@@ -1108,9 +1126,10 @@ int launch_stages(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t 
   Bufs<T> b = make_bufs<T>(L, state, a);
   const int g = L.grid;
   const int n = L.n;
-  constexpr int kA = WenoTile<T>::A, kL = WenoTile<T>::L, kWT = WenoTile<T>::THREADS;
-  const dim3 wg((n + kA - 1) / kA, (n + kL - 1) / kL, n);
-  const size_t wsm = weno_smem<T>();
+  constexpr int kA = WenoTile<T, 0>::A, kAyz = WenoTile<T, 1>::A, kL = WenoTile<T, 0>::L;
+  constexpr int kWT = WenoTile<T, 0>::THREADS;
+  const dim3 wg((n + kA - 1) / kA, (n + kL - 1) / kL, n), wgyz((n + kAyz - 1) / kAyz, (n + kL - 1) / kL, n);
+  const size_t wsm = weno_smem<T, 0>(), wsmyz = weno_smem<T, 1>();
   const dim3 g3 = sweep_grid(n), b3 = sweep_block();
   const dim3 gxe = sweep_grid_x<kSweepXEmf>(n);
   for (int st = 0; st < 5; ++st) {
@@ -1123,9 +1142,9 @@ int launch_stages(const FDLaunch& L, void* state, const FDArgs& a, cudaStream_t 
       fd_mark(L, FD_PH_WIND, s);
     }
     // z and y store their flux differences; x (last) applies the stage to Q
-    k_weno<T, 2><<<wg, kWT, wsm, s>>>(b, st);
+    k_weno<T, 2><<<wgyz, kWT, wsmyz, s>>>(b, st);
     fd_mark(L, FD_PH_WENO_Z, s);
-    k_weno<T, 1><<<wg, kWT, wsm, s>>>(b, st);
+    k_weno<T, 1><<<wgyz, kWT, wsmyz, s>>>(b, st);
     fd_mark(L, FD_PH_WENO_Y, s);
     k_weno<T, 0><<<wg, kWT, wsm, s>>>(b, st);
     fd_mark(L, FD_PH_WENO_X, s);
