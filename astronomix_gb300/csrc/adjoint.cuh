@@ -58,11 +58,29 @@ __device__ __forceinline__ void minmod_d(T a, T b, T* ga, T* gb) {
   *gb = s * wb * sgn(b);
 }
 
-// |v|^2 as the forward forms it (abs_velocity squared)
+// |v|^2 as the forward forms it (abs_velocity squared); FP32 skips the
+// square root and its square (the same value up to rounding)
 template <typename T, int DIM>
 __device__ __forceinline__ T vsq(const T* q) {
+  if constexpr (sizeof(T) == 4 && DIM >= 2) {
+    T s = q[1] * q[1] + q[2] * q[2];
+    if (DIM == 3) s = s + q[3] * q[3] + T(1e-20);
+    return s;
+  }
   const T u = abs_velocity<T, DIM>(q);
   return u * u;
+}
+
+// the wave-speed bounds' maxima and minima: NaN-propagating in FP64 as the
+// forward's, plain min/max instructions in FP32 (a NaN state has no
+// gradient worth keeping)
+template <typename T> __device__ __forceinline__ T vmax(T a, T b) {
+  if constexpr (sizeof(T) == 4) return fmaxf(a, b);
+  else return jmax(a, b);
+}
+template <typename T> __device__ __forceinline__ T vmin(T a, T b) {
+  if constexpr (sizeof(T) == 4) return fminf(a, b);
+  else return jmin(a, b);
 }
 
 // ------------------------------------------------------------ pointwise VJPs
@@ -136,8 +154,8 @@ __device__ __forceinline__ void hll_vjp(const T* qL, const T* qR, int d, T gamma
   prim_to_cons<T, DIM>(qL, UL, gamma);
   prim_to_cons<T, DIM>(qR, UR, gamma);
   const T a1 = uL + cL, a2 = uR + cR, b1 = uL - cL, b2 = uR - cR;
-  const T ma = jmax(a1, a2), mb = jmin(b1, b2);
-  const T SR = jmax(ma, T(0)), SL = jmin(mb, T(0));
+  const T ma = vmax(a1, a2), mb = vmin(b1, b2);
+  const T SR = vmax(ma, T(0)), SL = vmin(mb, T(0));
   const T rden = T(1) / (SR - SL);
   T lnum[NV], lFL[NV], lFR[NV], lUL[NV], lUR[NV];
   T lden = T(0), lSR = T(0), lSL = T(0);
@@ -323,7 +341,9 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
   }
   __syncthreads();
   // the limited slope D[m] = minmod(bd, fd) dx / 2 of every cell m in
-  // [-2, L+1], once (and in FP32 its partial derivatives)
+  // [-2, L+1], once, as the forward's reconstruction forms it (FP32:
+  // minmod of the differences by cases, /2; FP64: the reference's
+  // formula), and in FP32 its partial derivatives
   for (int e = threadIdx.x; e < W * A::UL; e += blockDim.x) {
     int w, m;
     split(e, A::UL, &w, &m);
@@ -331,14 +351,16 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       const T* sp = sP + (v * W + w) * A::PL + 1;  // cell m at sp[m]
-      const T bd = (sp[m] - sp[m - 1]) / dxT, fd = (sp[m + 1] - sp[m]) / dxT;
       const int o = (v * W + w) * A::UL + m;
-      sD[o] = limited(bd, fd, 0, dxT) * dxT / T(2);
+      sD[o] = half_slope(sp[m - 1], sp[m], sp[m + 1], 0, dxT);
       if (KEEP) {
-        T ga, gb;
-        minmod_d(bd, fd, &ga, &gb);
-        sGa[o] = ga;
-        sGb[o] = gb;
+        // d minmod / d(a, b) by cases: the smaller magnitude's weight (ties
+        // split equally) where a and b share a sign, else 0
+        const T a_ = sp[m] - sp[m - 1], b_ = sp[m + 1] - sp[m];
+        const bool same = (a_ > T(0) && b_ > T(0)) || (a_ < T(0) && b_ < T(0));
+        const T aa = Num<T>::abs_(a_), ab = Num<T>::abs_(b_);
+        sGa[o] = same ? (aa < ab ? T(1) : (aa == ab ? T(0.5) : T(0))) : T(0);
+        sGb[o] = same ? (ab < aa ? T(1) : (aa == ab ? T(0.5) : T(0))) : T(0);
       }
     }
   }
