@@ -233,14 +233,18 @@ struct AxisTile {
   static constexpr int J = KFAST ? DIM - 2 : DIM - 1;
   static constexpr int M = 3 - K - J;  // third axis (3D only)
   static constexpr int PL = L + 6, UL = L + 4, FL = L + 3;
+  static constexpr int LP = L + 1;  // pitch of the staged lPin of the tile's cells (odd)
   // one thread per face and per cell: every phase but the halo load runs in
   // a single round
   static constexpr int THREADS = W * (L + 4);
   template <typename T>
   static constexpr bool keep_partials() { return sizeof(T) == 4; }
-  template <typename T>
+  // FIRST (the pass that also does the stage's pointwise part) stages the
+  // stage output and its cotangent (UL cells), P0 and lP0 (the tile's cells)
+  template <typename T, bool FIRST>
   static constexpr size_t smem(int nv) {
-    return sizeof(T) * (size_t)nv * W * (PL + 2 * UL + 2 * FL + (keep_partials<T>() ? 2 * UL : 0));
+    return sizeof(T) * (size_t)nv * W *
+           (PL + 2 * UL + 2 * FL + (keep_partials<T>() ? 2 * UL : 0) + LP + (FIRST ? 2 * UL + 2 * LP : 0));
   }
 };
 
@@ -274,6 +278,14 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
   T* sLR = sLL + NV * W * A::FL;
   T* sGa = sLR + NV * W * A::FL;            // [NV][W][UL] d minmod / d backward difference (FP32)
   T* sGb = sGa + NV * W * A::UL;            // d minmod / d forward difference
+  // [NV][W][LP] lPin of the tile's cells, after the partials in FP32 and in
+  // their place in FP64; then (FIRST) P_out, lP_out [NV][W][UL] and P0, lP0
+  // [NV][W][LP]
+  T* sLin = KEEP ? sGb + NV * W * A::UL : sGa;
+  T* sQo = sLin + NV * W * A::LP;
+  T* sLo = sQo + NV * W * A::UL;
+  T* sP0 = sLo + NV * W * A::UL;
+  T* sLP0 = sP0 + NV * W * A::LP;
   const int n = g.n;
   const long long nc = g.nc;
   const T gamma = T(g.gamma);
@@ -305,7 +317,9 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
     if (A::KFAST) { *w = e / len; *m = e % len; } else { *w = e % W; *m = e / W; }
   };
 
-  // loads: P for m in [-3, L+2], lU for m in [-2, L+1]
+  // loads: P for m in [-3, L+2], lU for m in [-2, L+1].  The copies go
+  // straight to shared memory (cp.async), every one of a thread's issued
+  // before it waits for any: the pass is bound by their latency otherwise.
   for (int e = threadIdx.x; e < W * A::PL; e += blockDim.x) {
     int w, m;
     split(e, A::PL, &w, &m);
@@ -313,7 +327,7 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
     if (oJ + w >= n) continue;
     const long long c = cell(m, w);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) sP[(v * W + w) * A::PL + m + 3] = Pin[v * nc + c];
+    for (int v = 0; v < NV; ++v) cp_async_elem(sP + (v * W + w) * A::PL + m + 3, Pin + v * nc + c);
   }
   for (int e = threadIdx.x; e < W * A::UL; e += blockDim.x) {
     int w, m;
@@ -321,25 +335,58 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
     m -= 2;
     if (oJ + w >= n) continue;
     const long long c = cell(m, w);
-    T lu[NV];
-    if (FIRST) {
-      T q[NV], U[NV], lq[NV];
+    const int o = w * A::UL + m + 2;
+    if (!FIRST) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) { q[v] = Pout[v * nc + c]; lq[v] = lPout[v * nc + c]; }
+      for (int v = 0; v < NV; ++v) cp_async_elem(sU + v * W * A::UL + o, lU + v * nc + c);
+    } else {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        cp_async_elem(sQo + v * W * A::UL + o, Pout + v * nc + c);
+        cp_async_elem(sLo + v * W * A::UL + o, lPout + v * nc + c);
+      }
+    }
+  }
+  const bool want_lin = !FIRST || accumulate;
+  for (int e = threadIdx.x; e < W * L; e += blockDim.x) {
+    int w, l;
+    split(e, L, &w, &l);
+    if (oJ + w >= n || oK + l >= n) continue;
+    const long long c = cell(l, w);
+    const int o = w * A::LP + l;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      if (want_lin) cp_async_elem(sLin + v * W * A::LP + o, lPin + v * nc + c);
+      if (FIRST && P0) {
+        cp_async_elem(sP0 + v * W * A::LP + o, P0 + v * nc + c);
+        cp_async_elem(sLP0 + v * W * A::LP + o, lP0 + v * nc + c);
+      }
+    }
+  }
+  cp_async_commit();
+  cp_async_wait_all();
+  __syncthreads();
+  // FIRST: lU of the cells m in [-2, L+1] from the stage output and its
+  // cotangent (read by the face phase, after the next barrier)
+  if (FIRST) {
+    for (int e = threadIdx.x; e < W * A::UL; e += blockDim.x) {
+      int w, m;
+      split(e, A::UL, &w, &m);
+      if (oJ + w >= n) continue;
+      const int o = w * A::UL + m;
+      T q[NV], U[NV], lq[NV], lu[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) { q[v] = sQo[v * W * A::UL + o]; lq[v] = sLo[v * W * A::UL + o]; }
       prim_to_cons<T, DIM>(q, U, gamma);
       cons_to_prim_vjp<T, DIM>(U, lq, gamma, lu);
       if (P0) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) lu[v] = T(0.5) * lu[v];
       }
-    } else {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) lu[v] = lU[v * nc + c];
+      for (int v = 0; v < NV; ++v) sU[v * W * A::UL + o] = lu[v];
     }
-#pragma unroll
-    for (int v = 0; v < NV; ++v) sU[(v * W + w) * A::UL + m + 2] = lu[v];
   }
-  __syncthreads();
   // the limited slope D[m] = minmod(bd, fd) dx / 2 of every cell m in
   // [-2, L+1], once, as the forward's reconstruction forms it (FP32:
   // minmod of the differences by cases, /2; FP64: the reference's
@@ -433,16 +480,16 @@ k_stage_axis(AdjGrid<T> g, const T* Pin, const T* Pout, const T* P0, const T* lP
       if (P0) {
         T q0[NV], l0[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) { q0[v] = P0[v * nc + c]; l0[v] = T(0); }
+        for (int v = 0; v < NV; ++v) { q0[v] = sP0[(v * W + w) * A::LP + l]; l0[v] = T(0); }
         prim_to_cons_vjp<T, DIM>(q0, lu, gamma, l0);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) lP0[v * nc + c] += l0[v];
+        for (int v = 0; v < NV; ++v) lP0[v * nc + c] = sLP0[(v * W + w) * A::LP + l] + l0[v];
       }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) lPin[v * nc + c] = accumulate ? lPin[v * nc + c] + r[v] : r[v];
+      for (int v = 0; v < NV; ++v) lPin[v * nc + c] = accumulate ? sLin[(v * W + w) * A::LP + l] + r[v] : r[v];
     } else {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) lPin[v * nc + c] += r[v];
+      for (int v = 0; v < NV; ++v) lPin[v * nc + c] = sLin[(v * W + w) * A::LP + l] + r[v];
     }
   }
 }
@@ -539,8 +586,14 @@ k_mag_adj1(AdjGrid<T> g, const T* Z, const T* S, const T* lZn, T h, int midpoint
   const int o2 = (DIM == 3) ? b * A::T2 : 0;
   for (int e = threadIdx.x; e < HALO; e += blockDim.x) {
     const int e2 = e % H2, e1 = (e / H2) % H1, e0 = e / (H2 * H1);
-    const int i0 = ((o0 + e0 - 1) % n + n) % n, i1 = ((o1 + e1 - 1) % n + n) % n;
-    const int i2 = (DIM == 3) ? ((o2 + e2 - 1) % n + n) % n : 0;
+    // periodic halo index (g >= -1): compares instead of two divisions a coordinate
+    auto per = [n](int g) {
+      if (g < 0) g += n;
+      while (g >= n) g -= n;
+      return g;
+    };
+    const int i0 = per(o0 + e0 - 1), i1 = per(o1 + e1 - 1);
+    const int i2 = (DIM == 3) ? per(o2 + e2 - 1) : 0;
     const long long c = cell_index<DIM>(i0, i1, i2, n);
     T Ba[3], va[3];
     avg_at<T, DIM>(Z, S, c, nc, midpoint != 0, Ba, va);
@@ -764,7 +817,7 @@ inline int grid_for(long long nc) {
 template <typename T, int DIM, int K, bool FIRST>
 int axis_attr() {
   return (int)cudaFuncSetAttribute(k_stage_axis<T, DIM, K, FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)AxisTile<DIM, K>::template smem<T>(DIM + 2));
+                                   (int)AxisTile<DIM, K>::template smem<T, FIRST>(DIM + 2));
 }
 
 template <typename T, int DIM>
@@ -782,7 +835,7 @@ void launch_axis(const AdjGrid<T>& g, const T* Pin, const T* Pout, const T* P0, 
                  T* lP0, int accumulate, T h, cudaStream_t s) {
   using A = AxisTile<DIM, K>;
   const long long blocks = (long long)((g.n + A::L - 1) / A::L) * ((g.n + A::W - 1) / A::W) * (DIM == 3 ? g.n : 1);
-  k_stage_axis<T, DIM, K, FIRST><<<(unsigned)blocks, A::THREADS, A::template smem<T>(DIM + 2), s>>>(
+  k_stage_axis<T, DIM, K, FIRST><<<(unsigned)blocks, A::THREADS, A::template smem<T, FIRST>(DIM + 2), s>>>(
       g, Pin, Pout, P0, lPout, lU, lPin, lP0, accumulate, h);
 }
 
