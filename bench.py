@@ -79,7 +79,7 @@ def run_case(name, n=None):
     """Small, self-contained runs of the workloads for ncu captures:
     fdblast: the headline FD blast at --n^3 FP32, 2 steps (one warm-up);
     fd: the reference's FD WENO-CT arena blast 128^3 FP32, 2 steps; fv3d: FV Lax-Friedrichs MHD
-    blast 192^3 FP32, 2 steps (one launch); fvsplit: the same blast with the
+    blast (--n, default 192)^3 FP32, 2 steps (one launch); fvsplit: the same blast with the
     split MUSCL-Hancock scheme and HLLC; ensemble: 8 turbulent 2D MHD
     runs (128^2..512^2, t_end / 8) in one batched launch; adjoint: the 3D
     density-perturbation problem at 96^3 to t = 0.01, forward and backward
@@ -104,7 +104,7 @@ def run_case(name, n=None):
     elif name in ("fd", "fv3d", "fvsplit"):
         from astronomix_gb300.time_integration import get_plan
 
-        cfg, prm, rv, s = arena_blast(128 if name == "fd" else 192, "fv_split" if name == "fvsplit" else name[:2])
+        cfg, prm, rv, s = arena_blast(n or (128 if name == "fd" else 192), "fv_split" if name == "fvsplit" else name[:2])
         plan = get_plan(cfg, rv, s.shape, np.float32)
         dev = torch.from_numpy(s).cuda()
         st = torch.cuda.current_stream().cuda_stream
@@ -310,6 +310,7 @@ def time_arena(solver, n=256, steps=3):
     plan.reset(st.cuda_stream)
     plan.run_async(dev.data_ptr(), p, 2, st.cuda_stream)
     torch.cuda.synchronize()
+    before = plan.run(dev.data_ptr(), p, 0, st.cuda_stream)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(st)
     plan.run_async(dev.data_ptr(), p, steps, st.cuda_stream)
@@ -324,6 +325,18 @@ def time_arena(solver, n=256, steps=3):
     if solver in H200_S_PER_STEP:
         out["h200_published_s_per_step"] = H200_S_PER_STEP[solver]
         out["speedup_vs_h200_published"] = H200_S_PER_STEP[solver] / sps
+    if solver == "fv":
+        # FV 3D MHD: 4 (57 + 19 (k + 1)) algorithmic bytes per zone-update, k
+        # the fixed-point iterations per step of the timed steps
+        k = (info.magnetic_iterations - before.magnetic_iterations) / max(1, info.steps - before.steps)
+        bpz = 4 * (57 + 19 * (k + 1))
+        peak, src = hbm_peak()
+        gbs = bpz * n ** 3 / sps / 1e9
+        out["magnetic_iterations_mean"] = k
+        out["roofline"] = {"bound": "hbm", "kernel": "fv_run_kernel", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                           "frac": gbs / peak, "traffic": load_traffic("fv_run_kernel_blast256_fp32_step"),
+                           "note": "algorithmic %.0f B/zone-update (k = %.2f), peak %s; traffic = DRAM bytes per "
+                                   "step (ncu)" % (bpz, k, src)}
     return out
 
 
