@@ -631,8 +631,20 @@ __device__ __forceinline__ void muscl_states(const T* qm, const T* q0, const T* 
                                              int limiter, T* left, T* right) {
   constexpr int NV = DIM + 2, P = DIM + 1;
   T g[NV];
+  if constexpr (sizeof(T) == 4) {
+    if (limiter == 0) {
+      // FP32 MINMOD: the minmod of the differences, divided by dx once
+      const T rdx = T(1) / dxT;
 #pragma unroll
-  for (int v = 0; v < NV; ++v) g[v] = limited((q0[v] - qm[v]) / dxT, (qp[v] - q0[v]) / dxT, limiter, dxT);
+      for (int v = 0; v < NV; ++v) g[v] = minmod_cases(q0[v] - qm[v], qp[v] - q0[v]) * rdx;
+    } else {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) g[v] = limited((q0[v] - qm[v]) / dxT, (qp[v] - q0[v]) / dxT, limiter, dxT);
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) g[v] = limited((q0[v] - qm[v]) / dxT, (qp[v] - q0[v]) / dxT, limiter, dxT);
+  }
   const T rho = q0[0], u = q0[d];
   const T c = sound_speed(rho, q0[P], gamma);
   const T half = dt / T(2), dist = dxT / T(2);
