@@ -987,9 +987,9 @@ __device__ __forceinline__ bool wind_source(const FDArgs& a, int i, int j, int k
 }
 
 // The wind source of one stage over the cube of cells that holds the taper
-// (zero outside it), before k_update adds it to the right-hand side.  Its
-// own kernel, so that the FP64 arithmetic does not weigh on the update's
-// registers.
+// (zero outside it), from the stage's input, before the x WENO pass adds it
+// to the right-hand side.  Its own kernel, so that the FP64 arithmetic does
+// not weigh on the WENO kernel's registers.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_wind_source(Bufs<T> b, int stage) {
   FD_ACTIVE_OR_RETURN(b.ctl);

@@ -95,7 +95,7 @@ __device__ __forceinline__ void grav_states(const GravSrc<T>& a, const T* qm, co
   } else {
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const T d = limited((q0[v] - qm[v]) / dxT, (qp[v] - q0[v]) / dxT, a.limiter, dxT) * dxT / T(2);
+      const T d = half_slope(qm[v], q0[v], qp[v], a.limiter, dxT);
       lo[v] = q0[v] - d;
       hi[v] = q0[v] + d;
     }

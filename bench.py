@@ -817,6 +817,32 @@ def cpu_baseline_fd(budget_s=15.0, n=64):
                       "blast %d^3 FP32, %d steps in %.1f s" % (threads, n, steps, dt)}
 
 
+def cpu_fv_sample(cfg, prm, s, budget_s):
+    """The oracle's compiled restatement of the reference's unsplit FV step
+    (oracle/cpu/fv_step.cpp, equal to the NumPy oracle on the CPU tests) on
+    the state s (FP32), with every host core (OpenMP): one warm-up step, then
+    steps until budget_s.  Returns the cpu_baseline record."""
+    from oracle import cpu
+
+    P = np.ascontiguousarray(s.astype(np.float32))
+    prm = prm._replace(t_end=1e9)
+    cpu.fv_run(P, cfg, prm, max_steps=1)
+    steps, iters = 0, 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < budget_s:
+        iters += cpu.fv_run(P, cfg, prm, max_steps=1)[2]
+        steps += 1
+    dt = time.perf_counter() - t0
+    zones = int(np.prod(s.shape[1:]))
+    shape = "x".join(str(v) for v in s.shape[1:])
+    out = {"value": zones * steps / dt, "unit": "zone-updates/s", "cores": cpu.threads(), "kind": "port",
+           "sample": "compiled restatement of the reference's FV step (C++17, OpenMP, %d threads), %s FP32, "
+                     "%d steps in %.1f s" % (cpu.threads(), shape, steps, dt)}
+    if cfg.mhd:
+        out["magnetic_iterations_mean"] = iters / max(1, steps)
+    return out
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -956,6 +982,14 @@ def run_ours(args, rank, world):
     if rank != 0:
         return
     cpu = None if args.no_cpu_baseline else cpu_baseline_fd()
+    if not args.no_cpu_baseline:
+        from _cases import orszag_tang
+        if ot is not None:
+            cfg_, prm_, rv_, s_ = orszag_tang(n=256, dtype=np.float32)
+            ot["cpu_baseline"] = cpu_fv_sample(cfg_, prm_, s_, 8.0)
+        if "fv_lf_blast_fp32" in arena:
+            cfg_, prm_, rv_, s_ = arena_blast(64, "fv")
+            arena["fv_lf_blast_fp32"]["cpu_baseline"] = cpu_fv_sample(cfg_, prm_, s_, 8.0)
     config = workload_config(n)
     config["parallelism"] = "replicas" if world > 1 else "single"
     line = {
