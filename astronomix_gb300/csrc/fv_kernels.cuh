@@ -146,6 +146,18 @@ template <typename T> struct TileV<T, 2, 2> {
 
 constexpr int kFVThreads = 256;
 
+// 3D FP32 magnetic evaluation streamed along axis 0 (mag_stream): a plane
+// tile of kMS1 x kMS2 cells (axes 1, 2), one cell per thread, with a halo of
+// one; a ring of four planes of six values (averaged B, E = B x v) per cell
+// and two planes of the 13 inputs of each thread's own cell.
+constexpr int kMS1 = 8, kMS2 = 32;
+constexpr int kMSW2 = kMS2 + 2;
+constexpr int kMSP = (kMS1 + 2) * kMSW2;
+constexpr int kMSRing = 2 * kMS2 + 2 * kMS1;  // the plane's halo without its corners
+constexpr int kMSRaw = 13;                    // B_k, v_k, B0, v0, rho
+static_assert(kMS1 * kMS2 == kFVThreads, "one cell of the plane tile per thread");
+static_assert(kMSRing <= kFVThreads, "one halo entry per thread");
+
 template <typename T, int DIM, int V = 0>
 struct TileGeom {
   static constexpr int NV = DIM + 2;
@@ -175,7 +187,10 @@ struct TileGeom {
   static constexpr int M0 = T0 + 2, M1 = (DIM >= 2) ? T1 + 2 : 1, M2 = (DIM >= 3) ? T2 + 2 : 1;
   static constexpr int MHALO = M0 * M1 * M2;
   static constexpr size_t HYDRO_SMEM = sizeof(T) * (size_t)NV * (HALO + FREG + SREG);
-  static constexpr size_t MAG_SMEM = sizeof(T) * (size_t)6 * MHALO;
+  static constexpr size_t MAG_TILE_SMEM = sizeof(T) * (size_t)6 * MHALO;
+  static constexpr size_t MAG_STREAM_SMEM =
+      (DIM == 3 && V == 0 && sizeof(T) == 4) ? sizeof(T) * ((size_t)4 * 6 * kMSP + (size_t)2 * kMSRaw * kFVThreads) : 0;
+  static constexpr size_t MAG_SMEM = MAG_TILE_SMEM > MAG_STREAM_SMEM ? MAG_TILE_SMEM : MAG_STREAM_SMEM;
   static constexpr size_t SMEM = HYDRO_SMEM > MAG_SMEM ? HYDRO_SMEM : MAG_SMEM;
   // VAN_ALBADA_PP: the limited differences of every axis for the tile and a
   // halo of 1, after the hydro arrays
@@ -1080,16 +1095,204 @@ __device__ __forceinline__ void mag_tile(const FVArgs<T>& a, const T* state, con
   *change_io = change;
 }
 
+// A cell's inputs to one evaluation of the fixed-point map.
+template <typename T>
+struct MagRaw {
+  T Bk[3], vk[3], B0[3], v0[3];
+};
+
+// Planes per work item of mag_stream: the run length that minimises (rounds of
+// work items over the grid) x (planes staged per item, the run plus two).
+__device__ __forceinline__ int mag_stream_run(int n, int grid) {
+  const long long cols = (long long)((n + kMS1 - 1) / kMS1) * ((n + kMS2 - 1) / kMS2);
+  int best = n;
+  long long best_cost = -1;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int c = (i == 7) ? n : (8 << (i / 2)) + ((i & 1) ? (4 << (i / 2)) : 0);  // 8 12 16 24 32 48 64, n
+    const int L = c < n ? c : n;
+    const long long items = cols * ((n + L - 1) / L);
+    const long long cost = ((items + grid - 1) / grid) * (L + 2);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = L;
+    }
+  }
+  return best;
+}
+
+// One 3D evaluation of the fixed-point map with the arithmetic of mag_tile,
+// streamed along axis 0 (FP32).  A work item is a column of kMS1 x kMS2 cells
+// (axes 1, 2) over a run of planes; the averaged B and E = B x v of four
+// consecutive planes, each with its axis-1/2 halo (no corners: the curls read
+// no diagonal neighbour), sit in a shared-memory ring.  Each thread loads its
+// own cell's inputs once, two planes before the plane is updated (the loads
+// are in flight while the current plane is updated), and parks them in
+// shared memory for the update: a cell's fields are read once per evaluation
+// (plus the halo of the column and two planes per run) instead of once per
+// halo-1 tile that covers it (2.4 times with 4 x 4 x 32 tiles).
+template <typename T>
+__device__ __forceinline__ void mag_stream(const FVArgs<T>& a, const T* state, const T* src, T* dst, T dt,
+                                           T* ring, T* change_io) {
+  T* raw = ring + 4 * 6 * kMSP;  // [2][kMSRaw][kFVThreads]
+  const long long nc = a.ncells;
+  const int n = a.n;
+  const T dx = T(a.dx);
+  const T hdx = T(0.5 * a.inv_dx);
+  const bool midpoint = (a.integrator == 0);
+  const AxisMap<3> amap(a);
+  const int L = mag_stream_run(n, gridDim.x);
+  const int C1 = (n + kMS1 - 1) / kMS1, C2 = (n + kMS2 - 1) / kMS2;
+  const long long items = (long long)C1 * C2 * ((n + L - 1) / L);
+  const int t = threadIdx.x;
+  const int c1 = t / kMS2, c2 = t % kMS2;
+  const int hOwn = (c1 + 1) * kMSW2 + (c2 + 1);
+  // this thread's halo entry (threads below kMSRing): the rows beside the
+  // tile along axis 1, then the columns beside it along axis 2
+  const bool has_ring = t < kMSRing;
+  int r1, r2;
+  if (t < kMS2) { r1 = -1; r2 = t; }
+  else if (t < 2 * kMS2) { r1 = kMS1; r2 = t - kMS2; }
+  else if (t < 2 * kMS2 + kMS1) { r1 = t - 2 * kMS2; r2 = -1; }
+  else { r1 = t - 2 * kMS2 - kMS1; r2 = kMS2; }
+  const int hRing = (r1 + 1) * kMSW2 + (r2 + 1);
+  T change = *change_io;
+
+  auto load = [&](long long c, MagRaw<T>& r) { load_iter<T, 3>(state, src, c, nc, r.Bk, r.vk, r.B0, r.v0); };
+  // the own cell's inputs of plane q into raw slot q & 1
+  auto park = [&](int sl, const MagRaw<T>& r, T rho) {
+    T* d = raw + sl * (kMSRaw * kFVThreads) + t;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      d[(0 + i) * kFVThreads] = r.Bk[i];
+      d[(3 + i) * kFVThreads] = r.vk[i];
+      d[(6 + i) * kFVThreads] = r.B0[i];
+      d[(9 + i) * kFVThreads] = r.v0[i];
+    }
+    d[12 * kFVThreads] = rho;
+  };
+  auto put = [&](T* sl, int h, const MagRaw<T>& r) {
+    T Ba[3], va[3], E[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      Ba[i] = midpoint ? (r.Bk[i] + r.B0[i]) / T(2) : r.Bk[i];
+      va[i] = midpoint ? (r.vk[i] + r.v0[i]) / T(2) : r.vk[i];
+    }
+    cross3(Ba, va, E);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      sl[i * kMSP + h] = Ba[i];
+      sl[(3 + i) * kMSP + h] = E[i];
+    }
+  };
+
+  for (long long item = blockIdx.x; item < items; item += gridDim.x) {
+    const int t2 = (int)(item % C2);
+    const int t1 = (int)((item / C2) % C1);
+    const int lo = (int)(item / ((long long)C2 * C1)) * L;
+    const int hi = lo + L < n ? lo + L : n;
+    const int g1 = t1 * kMS1 + c1, g2 = t2 * kMS2 + c2;
+    const bool valid = g1 < n && g2 < n;
+    bool fl;
+    const int j1 = amap(1, g1, &fl), j2 = amap(2, g2, &fl);
+    const int k1 = amap(1, t1 * kMS1 + r1, &fl), k2 = amap(2, t2 * kMS2 + r2, &fl);
+    auto own_cell = [&](int q) { return cell_index<3>(amap(0, q, &fl), j1, j2, n); };
+    auto ring_cell = [&](int q) { return cell_index<3>(amap(0, q, &fl), k1, k2, n); };
+    auto slot = [&](int q) { return ring + ((q - lo + 1) & 3) * (6 * kMSP); };
+
+    MagRaw<T> R, Q;
+    T rho = T(0);
+    // planes lo - 1, lo, lo + 1 (hi >= lo + 1: every run has a plane)
+#pragma unroll 1
+    for (int q = lo - 1; q <= lo + 1; ++q) {
+      const long long c = own_cell(q);
+      load(c, R);
+      if (q >= lo) rho = state[c];
+      if (has_ring) load(ring_cell(q), Q);
+      put(slot(q), hOwn, R);
+      if (has_ring) put(slot(q), hRing, Q);
+      if (q >= lo) park((q - lo) & 1, R, rho);
+    }
+    __syncthreads();
+
+#pragma unroll 1
+    for (int p = lo; p < hi; ++p) {
+      const bool more = p + 2 <= hi;
+      if (more) {
+        const long long c = own_cell(p + 2);
+        load(c, R);
+        rho = state[c];
+        if (has_ring) load(ring_cell(p + 2), Q);
+      }
+      if (valid) {
+        const T* r0 = raw + ((p - lo) & 1) * (kMSRaw * kFVThreads) + t;
+        const T* Sm = slot(p - 1);
+        const T* S0 = slot(p);
+        const T* Sp = slot(p + 1);
+        // d(F_i)/d(x_k) = 0.5 (F_i[+] - F_i[-]) / dx  (_vector_maths.py:55-100);
+        // FP32 multiplies by 0.5 / dx instead of dividing
+        auto dF = [&](int f, int i, int k) {
+          const int o = (f + i) * kMSP + hOwn;
+          const T d = (k == 0) ? Sp[o] - Sm[o] : (k == 1) ? S0[o + kMSW2] - S0[o - kMSW2] : S0[o + 1] - S0[o - 1];
+          if constexpr (sizeof(T) == 4) return d * hdx;
+          else return T(0.5) * d / dx;
+        };
+        T curlE[3], curlB[3];
+        curlE[0] = dF(3, 2, 1) - dF(3, 1, 2);
+        curlE[1] = dF(3, 0, 2) - dF(3, 2, 0);
+        curlE[2] = dF(3, 1, 0) - dF(3, 0, 1);
+        curlB[0] = dF(0, 2, 1) - dF(0, 1, 2);
+        curlB[1] = dF(0, 0, 2) - dF(0, 2, 0);
+        curlB[2] = dF(0, 1, 0) - dF(0, 0, 1);
+        T Ba[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) Ba[i] = S0[i * kMSP + hOwn];
+        T phi2[3];
+        cross3(Ba, curlB, phi2);
+        const T rho0 = r0[12 * kFVThreads];
+        T Bn[3], vn[3], dBs[3], dvs[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          Bn[i] = r0[(6 + i) * kFVThreads] - dt * curlE[i];
+          vn[i] = r0[(9 + i) * kFVThreads] - dt * (phi2[i] / rho0);
+          dBs[i] = r0[(0 + i) * kFVThreads] - Bn[i];
+          dvs[i] = r0[(3 + i) * kFVThreads] - vn[i];
+        }
+        const T dB = Num<T>::sqrt_(sq(dBs[0]) + sq(dBs[1]) + sq(dBs[2]));
+        const T dv = Num<T>::sqrt_(sq(dvs[0]) + sq(dvs[1]) + sq(dvs[2]));
+        change = nanmax(change, nanmax(dB, dv));
+        const long long c = cell_index<3>(p, g1, g2, n);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          dst[i * nc + c] = Bn[i];
+          dst[(3 + i) * nc + c] = vn[i];
+        }
+      }
+      if (more) {
+        put(slot(p + 2), hOwn, R);
+        if (has_ring) put(slot(p + 2), hRing, Q);
+        park((p + 2 - lo) & 1, R, rho);  // the slot plane p's inputs leave
+      }
+      __syncthreads();
+    }
+  }
+  *change_io = change;
+}
+
 template <typename T, int DIM>
 __device__ __noinline__ void phase_mag_iterate(const FVArgs<T>& a, const T* state, const T* src, T* dst, T dt,
                                                unsigned long long* slot, double* red, T* smem) {
-  using G = TileGeom<T, DIM>;
-  const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
   T change = T(0);
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    int o[3];
-    tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
-    mag_tile<T, DIM>(a, state, o, src, dst, dt, smem, &change);
+  if constexpr (DIM == 3 && sizeof(T) == 4) {
+    mag_stream<T>(a, state, src, dst, dt, smem, &change);
+  } else {
+    using G = TileGeom<T, DIM>;
+    const long long ntiles = fv_num_tiles<DIM>(a.n, G::T0, G::T1, G::T2);
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+      int o[3];
+      tile_origin<DIM>(tile, a.n, G::T0, G::T1, G::T2, o);
+      mag_tile<T, DIM>(a, state, o, src, dst, dt, smem, &change);
+    }
   }
   const double r = block_max<double>((double)change, red);
   if (threadIdx.x == 0) atomic_max_nonneg(slot, r);

@@ -114,6 +114,22 @@ def test_mhd_3d_fp64(cuda, riemann):
     assert rel_err(got, ref) < FP64_TOL
 
 
+@pytest.mark.parametrize("n,t_end", [(12, 0.03), (40, 0.008)])
+def test_mhd_3d_fp32_every_row(cuda, n, t_end):
+    """The FP32 3D magnetic evaluation streams 8 x 32 columns along the
+    first axis in runs of planes: 12 cells per axis give a partial column
+    and a partial run, 40 a full and a partial column along the last axis
+    and five runs.  Every row within 1e-5 (relative L1) of the FP64 oracle."""
+    cfg, prm, rv, s = smooth_random(3, n, seed=13, mhd=True, riemann=HLL, t_end=t_end, dtype=np.float32)
+    got = amx.time_integration(s.copy(), cfg, prm, rv)
+    rec = {}
+    ref64 = odriver.time_integration(s.astype(np.float64), cfg, prm, rv, record=rec)
+    assert rec["steps"] >= 2 and sum(rec["magnetic_iterations"]) > 0
+    assert got.dtype == np.float32
+    for row in range(got.shape[0]):
+        assert rel_l1(got, ref64, row=row) < 1e-5, row
+
+
 def test_orszag_tang_fp32_l1(cuda):
     cfg, prm, rv, s = orszag_tang(n=64, t_end=0.05, dtype=np.float32)
     got = amx.time_integration(s.copy(), cfg, prm, rv)
