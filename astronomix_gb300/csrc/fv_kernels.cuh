@@ -155,6 +155,11 @@ constexpr int kMSW2 = kMS2 + 2;
 constexpr int kMSP = (kMS1 + 2) * kMSW2;
 constexpr int kMSRing = 2 * kMS2 + 2 * kMS1;  // the plane's halo without its corners
 constexpr int kMSRaw = 13;                    // B_k, v_k, B0, v0, rho
+// planes ahead of the update whose rows mag_stream prefetches into L2 (0: none)
+#ifndef AMX_MAG_PF
+#define AMX_MAG_PF 4
+#endif
+
 static_assert(kMS1 * kMS2 == kFVThreads, "one cell of the plane tile per thread");
 static_assert(kMSRing <= kFVThreads, "one halo entry per thread");
 
@@ -1126,11 +1131,11 @@ __device__ __forceinline__ int mag_stream_run(int n, int grid) {
 // (axes 1, 2) over a run of planes; the averaged B and E = B x v of four
 // consecutive planes, each with its axis-1/2 halo (no corners: the curls read
 // no diagonal neighbour), sit in a shared-memory ring.  Each thread loads its
-// own cell's inputs once, two planes before the plane is updated (the loads
-// are in flight while the current plane is updated), and parks them in
-// shared memory for the update: a cell's fields are read once per evaluation
-// (plus the halo of the column and two planes per run) instead of once per
-// halo-1 tile that covers it (2.4 times with 4 x 4 x 32 tiles).
+// own cell's inputs once, two planes before the plane is updated, and parks
+// them in shared memory for the update: a cell's fields are read once per
+// evaluation (plus the halo of the column and two planes per run) instead of
+// once per halo-1 tile that covers it (2.4 times with 4 x 4 x 32 tiles).  The
+// rows of the plane AMX_MAG_PF planes ahead are prefetched into L2.
 template <typename T>
 __device__ __forceinline__ void mag_stream(const FVArgs<T>& a, const T* state, const T* src, T* dst, T dt,
                                            T* ring, T* change_io) {
@@ -1156,6 +1161,17 @@ __device__ __forceinline__ void mag_stream(const FVArgs<T>& a, const T* state, c
   else if (t < 2 * kMS2 + kMS1) { r1 = t - 2 * kMS2; r2 = -1; }
   else { r1 = t - 2 * kMS2 - kMS1; r2 = kMS2; }
   const int hRing = (r1 + 1) * kMSW2 + (r2 + 1);
+  // the row this thread prefetches into L2 for a plane: threads below 13 x
+  // kMS1 take the tile's rows of the 13 input arrays (B0, v0, iterate B and
+  // v, density), the next 24 the two halo rows of the 12 vector arrays
+  int pa = -1, pr = 0;
+  if (t < kMSRaw * kMS1) { pa = t / kMS1; pr = t % kMS1; }
+  else if (t < kMSRaw * kMS1 + 24) { const int u = t - kMSRaw * kMS1; pa = u >> 1; pr = (u & 1) ? kMS1 : -1; }
+  const T* parr = nullptr;
+  if (pa >= 0 && pa < 3) parr = state + (5 + pa) * nc;
+  else if (pa >= 3 && pa < 6) parr = state + (1 + pa - 3) * nc;
+  else if (pa >= 6 && pa < 12) parr = src ? src + (pa - 6) * nc : nullptr;
+  else if (pa == 12) parr = state;
   T change = *change_io;
 
   auto load = [&](long long c, MagRaw<T>& r) { load_iter<T, 3>(state, src, c, nc, r.Bk, r.vk, r.B0, r.v0); };
@@ -1199,6 +1215,13 @@ __device__ __forceinline__ void mag_stream(const FVArgs<T>& a, const T* state, c
     auto own_cell = [&](int q) { return cell_index<3>(amap(0, q, &fl), j1, j2, n); };
     auto ring_cell = [&](int q) { return cell_index<3>(amap(0, q, &fl), k1, k2, n); };
     auto slot = [&](int q) { return ring + ((q - lo + 1) & 3) * (6 * kMSP); };
+    const int pj1 = amap(1, t1 * kMS1 + pr, &fl);
+    auto prefetch = [&](int q) {
+      if (AMX_MAG_PF > 0 && parr && q <= hi)
+        asm volatile("prefetch.L2 [%0];" ::"l"(parr + cell_index<3>(amap(0, q, &fl), pj1, t2 * kMS2, n)));
+    };
+#pragma unroll 1
+    for (int q = lo + 2; q < lo + AMX_MAG_PF; ++q) prefetch(q);
 
     MagRaw<T> R, Q;
     T rho = T(0);
@@ -1217,13 +1240,8 @@ __device__ __forceinline__ void mag_stream(const FVArgs<T>& a, const T* state, c
 
 #pragma unroll 1
     for (int p = lo; p < hi; ++p) {
+      prefetch(p + AMX_MAG_PF);
       const bool more = p + 2 <= hi;
-      if (more) {
-        const long long c = own_cell(p + 2);
-        load(c, R);
-        rho = state[c];
-        if (has_ring) load(ring_cell(p + 2), Q);
-      }
       if (valid) {
         const T* r0 = raw + ((p - lo) & 1) * (kMSRaw * kFVThreads) + t;
         const T* Sm = slot(p - 1);
@@ -1268,7 +1286,14 @@ __device__ __forceinline__ void mag_stream(const FVArgs<T>& a, const T* state, c
           dst[(3 + i) * nc + c] = vn[i];
         }
       }
+      // the inputs of plane p + 2, after the update of plane p (loading them
+      // before it, to overlap, spills at this kernel's 80 registers and
+      // measured slower); the L2 prefetch above hides their memory latency
       if (more) {
+        const long long c = own_cell(p + 2);
+        load(c, R);
+        rho = state[c];
+        if (has_ring) load(ring_cell(p + 2), Q);
         put(slot(p + 2), hOwn, R);
         if (has_ring) put(slot(p + 2), hRing, Q);
         park((p + 2 - lo) & 1, R, rho);  // the slot plane p's inputs leave
