@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--no-gravity", action="store_true", help="skip the self-gravity collapse workload")
     ap.add_argument("--no-l1", action="store_true", help="skip the full FP32 and FP64 runs to t_end (L1 error)")
     ap.add_argument("--no-ot", action="store_true", help="skip the Orszag-Tang 512^2 FV workload")
+    ap.add_argument("--cpu-fp32-l1", type=int, default=0, metavar="N",
+                    help="print the FP32-vs-FP64 L1 of the CPU restatement on Orszag-Tang N^2 to t = 0.5 and exit")
     ap.add_argument("--case", default=None, choices=["fdblast", "fd", "fdsrc", "fv3d", "fvsplit", "ensemble",
                                                      "adjoint", "gravity"],
                     help="run one small case of a secondary workload and exit (for profilers)")
@@ -843,6 +845,29 @@ def cpu_fv_sample(cfg, prm, s, budget_s):
     return out
 
 
+def cpu_fp32_l1(n, t_end=0.5):
+    """FP32-vs-FP64 relative L1 density error of the oracle's compiled
+    restatement of the reference's FV step (IEEE arithmetic, no contraction)
+    on Orszag-Tang n^2 to t_end: the accuracy of a faithful FP32 run of the
+    scheme, against which the GPU's FP32 figure is read.  CPU only."""
+    from _cases import orszag_tang
+    from oracle import cpu
+
+    out, res = {"workload": "Orszag-Tang %dx%d to t = %g, oracle/cpu/fv_step.cpp" % (n, n, t_end)}, {}
+    for dt in (np.float32, np.float64):
+        cfg, prm, rv, s = orszag_tang(n=n, t_end=t_end, dtype=dt)
+        s = np.ascontiguousarray(s.astype(dt))
+        t0 = time.perf_counter()
+        t, steps, iters = cpu.fv_run(s, cfg, prm)
+        res[dt.__name__] = s[0].astype(np.float64)
+        out[dt.__name__] = {"t": t, "steps": steps, "magnetic_iterations": iters,
+                            "seconds": time.perf_counter() - t0}
+    out["rel_l1_density_fp32_vs_fp64"] = float(np.abs(res["float32"] - res["float64"]).sum() /
+                                               np.abs(res["float64"]).sum())
+    out["cores"] = cpu.threads()
+    return out
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -1037,6 +1062,9 @@ def run_ours(args, rank, world):
 
 def main():
     args = parse()
+    if args.cpu_fp32_l1:
+        print(json.dumps(cpu_fp32_l1(args.cpu_fp32_l1)))
+        return
     if args.case:
         run_case(args.case, args.n)
         return
