@@ -71,7 +71,7 @@ def parse():
     ap.add_argument("--no-ot", action="store_true", help="skip the Orszag-Tang 512^2 FV workload")
     ap.add_argument("--cpu-fp32-l1", type=int, default=0, metavar="N",
                     help="print the FP32-vs-FP64 L1 of the CPU restatement on Orszag-Tang N^2 to t = 0.5 and exit")
-    ap.add_argument("--case", default=None, choices=["fdblast", "fd", "fdsrc", "fv3d", "fvsplit", "ensemble",
+    ap.add_argument("--case", default=None, choices=["fdblast", "fd", "fdsrc", "fv3d", "fv3dseams", "fvsplit", "ensemble",
                                                      "adjoint", "gravity"],
                     help="run one small case of a secondary workload and exit (for profilers)")
     return ap.parse_args()
@@ -81,7 +81,9 @@ def run_case(name, n=None):
     """Small, self-contained runs of the workloads for ncu captures:
     fdblast: the headline FD blast at --n^3 FP32, 2 steps (one warm-up);
     fd: the reference's FD WENO-CT arena blast 128^3 FP32, 2 steps; fv3d: FV Lax-Friedrichs MHD
-    blast (--n, default 192)^3 FP32, 2 steps (one launch); fvsplit: the same blast with the
+    blast (--n, default 192)^3 FP32, 2 steps (one launch); fv3dseams: the same blast, the RK2 hydro
+    seam and the magnetic seam called twice each (four launches; ncu -s 2 -c 2 takes the second
+    pair); fvsplit: the same blast with the
     split MUSCL-Hancock scheme and HLLC; ensemble: 8 turbulent 2D MHD
     runs (128^2..512^2, t_end / 8) in one batched launch; adjoint: the 3D
     density-perturbation problem at 96^3 to t = 0.01, forward and backward
@@ -113,6 +115,20 @@ def run_case(name, n=None):
         plan.reset(st)
         info = plan.run(dev.data_ptr(), _native.make_params(prm), 2, st)
         print(json.dumps({"case": name, "steps": info.steps, "status": info.status}))
+    elif name == "fv3dseams":
+        from astronomix_gb300.time_integration import get_plan
+
+        cfg, prm, rv, s = arena_blast(n or 192, "fv")
+        plan = get_plan(cfg, rv, s.shape, np.float32)
+        dev = torch.from_numpy(s).cuda()
+        st = torch.cuda.current_stream().cuda_stream
+        plan.reset(st)
+        p = _native.make_params(prm)
+        for _ in range(2):
+            plan.hydro_rk2(dev.data_ptr(), p, 1e-5, st)
+            plan.magnetic_update(dev.data_ptr(), p, 2e-4, st)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": name, "status": plan.status(), "finite": bool(torch.isfinite(dev).all())}))
     elif name == "fdsrc":
         from astronomix_gb300.time_integration import get_plan
         from astronomix_gb300.option_classes import (WindConfig, WindParams, TurbulentForcingConfig,
