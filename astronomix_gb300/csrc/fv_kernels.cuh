@@ -191,7 +191,11 @@ struct TileGeom {
   // magnetic tile: halo 1, six values per cell (averaged B and E = B x v)
   static constexpr int M0 = T0 + 2, M1 = (DIM >= 2) ? T1 + 2 : 1, M2 = (DIM >= 3) ? T2 + 2 : 1;
   static constexpr int MHALO = M0 * M1 * M2;
-  static constexpr size_t HYDRO_SMEM = sizeof(T) * (size_t)NV * (HALO + FREG + SREG);
+  // FP32 3D: the halo tile starts two values into the buffer, so that the
+  // interior of every halo row (the tile's own cells along axis 2) sits on a
+  // 16-byte boundary for the 16-byte copies of hydro_tile
+  static constexpr int SP_OFF = (DIM == 3 && V == 0 && sizeof(T) == 4) ? 2 : 0;
+  static constexpr size_t HYDRO_SMEM = sizeof(T) * ((size_t)NV * (HALO + FREG + SREG) + SP_OFF);
   static constexpr size_t MAG_TILE_SMEM = sizeof(T) * (size_t)6 * MHALO;
   static constexpr size_t MAG_STREAM_SMEM =
       (DIM == 3 && V == 0 && sizeof(T) == 4) ? sizeof(T) * ((size_t)4 * 6 * kMSP + (size_t)2 * kMSRaw * kFVThreads) : 0;
@@ -414,24 +418,58 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
   const int limiter = a.limiter;
   const bool lm = a.lm != 0;
   const AxisMap<DIM> amap(a);
-  T* sP = smem;                        // [NV][HALO]
-  T* sF = smem + NV * G::HALO;         // [NV][FMAX]
+  T* sP = smem + G::SP_OFF;            // [NV][HALO]
+  T* sF = sP + NV * G::HALO;           // [NV][FMAX]
   T* sD = sF + NV * G::FMAX;           // [NV][SMAX] slopes (already * dx / 2)
 
   // ---- load the halo'd tile of primitives (boundary-mapped)
   if constexpr (DIM == 3) {
-    // 3D (4.5 halo cells per tile cell, HBM-bound): every thread issues all
-    // of its copies (cp.async) before waiting for any; a reflective wall's
-    // sign flips are applied afterwards by the thread that copied the cell
-    for (int e = threadIdx.x; e < G::HALO; e += blockDim.x) {
-      const int h2 = e % G::H2;
-      const int h1 = (e / G::H2) % G::H1;
-      const int h0 = e / (G::H2 * G::H1);
-      bool f = false;
-      const long long c =
-          cell_index<DIM>(amap(0, o[0] + h0 - 2, &f), amap(1, o[1] + h1 - 2, &f), amap(2, o[2] + h2 - 2, &f), n);
+    // 3D (4.5 halo cells per tile cell): every thread issues all of its
+    // copies (cp.async) before waiting for any; a reflective wall's sign
+    // flips are applied afterwards.  FP32, when the grid and the input
+    // allow it: the tile's own cells of each halo row (axis 2, in range and
+    // 16-byte aligned) go as 16-byte copies, four values each, and the two
+    // halo cells at either end as mapped single values: the index arithmetic
+    // is done per row and per copy of four rather than per value.
+    bool rows = false;
+    if constexpr (G::SP_OFF == 2) {
+      static_assert(G::T2 % 4 == 0 && G::H2 == G::T2 + 4 && G::HALO % 4 == 0 && G::H2 % 4 == 0,
+                    "16-byte row copies: the row interior starts two values in");
+      rows = (n % 4 == 0) && (o[2] + G::T2 <= n) && ((reinterpret_cast<unsigned long long>(Pin) & 15ull) == 0);
+    }
+    if (rows) {
+      constexpr int Q = G::T2 / 4;      // 16-byte copies per row
+      constexpr int SLOTS = Q + 4;      // and the four mapped end cells
+      constexpr int NROWS = G::H0 * G::H1;
+      for (int it = threadIdx.x; it < NROWS * SLOTS; it += blockDim.x) {
+        const int row = it / SLOTS, sl = it % SLOTS;
+        const int h0 = row / G::H1, h1 = row % G::H1;
+        bool f = false;
+        const long long base = ((long long)amap(0, o[0] + h0 - 2, &f) * n + amap(1, o[1] + h1 - 2, &f)) * n;
+        if (sl < Q) {
+          const int j = 2 + 4 * sl;  // halo column of the copy's first value
+          const long long c = base + o[2] + 4 * sl;
 #pragma unroll
-      for (int v = 0; v < NV; ++v) cp_async_elem(sP + v * G::HALO + e, Pin + v * nc + c);
+          for (int v = 0; v < NV; ++v) cp_async_16(sP + v * G::HALO + row * G::H2 + j, Pin + v * nc + c);
+        } else {
+          const int k = sl - Q;                     // 0, 1: left of the tile; 2, 3: right
+          const int j = (k < 2) ? k : G::T2 + k;    // halo columns 0, 1, T2 + 2, T2 + 3
+          const long long c = base + amap(2, o[2] + j - 2, &f);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) cp_async_elem(sP + v * G::HALO + row * G::H2 + j, Pin + v * nc + c);
+        }
+      }
+    } else {
+      for (int e = threadIdx.x; e < G::HALO; e += blockDim.x) {
+        const int h2 = e % G::H2;
+        const int h1 = (e / G::H2) % G::H1;
+        const int h0 = e / (G::H2 * G::H1);
+        bool f = false;
+        const long long c =
+            cell_index<DIM>(amap(0, o[0] + h0 - 2, &f), amap(1, o[1] + h1 - 2, &f), amap(2, o[2] + h2 - 2, &f), n);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) cp_async_elem(sP + v * G::HALO + e, Pin + v * nc + c);
+      }
     }
     cp_async_commit();
     cp_async_wait_all();
@@ -471,7 +509,7 @@ __device__ __forceinline__ void hydro_tile(const FVArgs<T>& a, const int* o, con
 
   // ---- VAN_ALBADA_PP: the rescaled differences of every axis for the tile
   // and a halo of 1, before any face needs them (reconstruction.py:134-394)
-  T* sPP = smem + NV * (G::HALO + G::FREG + G::SREG);  // [DIM][NV][BOX]
+  T* sPP = sP + NV * (G::HALO + G::FREG + G::SREG);  // [DIM][NV][BOX]
   if (PP) {
     pp_prepass<T, DIM, V>(a, sP, sPP, ppC);
     __syncthreads();
