@@ -431,10 +431,19 @@ def time_ensemble(num_runs=64, sequential=True):
     zu = sum(i.steps * s[-1] * s[-2] for i, s in zip(infos, shapes))
     iters = sum(i.magnetic_iterations for i in infos) / max(1, sum(i.steps for i in infos))
     ok = all(i.status == 0 for i in infos) and all(abs(i.t - m[1].t_end) < 1e-9 for i, m in zip(infos, ms))
+    # algorithmic bytes: each run's own steps and fixed-point iterations in
+    # the 2D formula, 4 (46 + 16 (k + 1)) bytes a zone-update
+    nbytes = sum(4 * s[-1] * s[-2] * (46 * i.steps + 16 * (i.magnetic_iterations + i.steps))
+                 for i, s in zip(infos, shapes))
+    peak, peak_src = hbm_peak()
     out = {"runs": num_runs, "grids": sorted(set(s[-1] for s in shapes)), "cells_total": sum(s[-1] * s[-2] for s in shapes),
            "zone_updates": zu, "seconds": sec, "zone_updates_per_s": zu / sec, "lock_steps": lock,
            "magnetic_iterations_mean": iters, "tiling": tiling, "tune_s": tune_s, "graph": True, "ok": ok,
-           "launches": 2}
+           "launches": 2,
+           "roofline": {"bound": "hbm", "kernel": "fv_batch_kernel", "achieved": nbytes / sec / 1e9, "peak": peak,
+                        "unit": "GB/s", "frac": nbytes / sec / 1e9 / peak, "traffic": None,
+                        "note": "algorithmic bytes summed over the runs with their own steps and fixed-point "
+                                "iterations, 4 (46 + 16 (k + 1)) B a zone-update; peak %s" % peak_src}}
     if sequential:
         seq_s = 0.0
         for m, h in zip(ms, host):
