@@ -22,6 +22,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--ex
 
 # the slowest units first, so that the parallel build finishes early
 SOURCES = ["fv_f32_schemes.cu", "fv_f64_schemes.cu", "fv_batch_f32.cu", "fv_batch_f32_alt.cu", "adjoint_f32.cu",
+           "fv_f32_split_am.cu", "fv_f64_split_am.cu",
            "adjoint_f64.cu", "amx_api.cu", "fv_f32.cu", "fv_f64.cu", "fd.cu", "fd_f32.cu", "fd_f64.cu",
            "fv_batch_f64.cu", "batch.cu", "adjoint.cu", "gravity.cu", "gravity_f32.cu", "forcing.cu", "diag.cu"]
 
@@ -30,7 +31,8 @@ SOURCES = ["fv_f32_schemes.cu", "fv_f64_schemes.cu", "fv_batch_f32.cu", "fv_batc
 # operations for round-off parity with the reference.
 _FAST = ["-prec-div=false", "-prec-sqrt=false"]
 EXTRA_FLAGS = {"fv_f32.cu": _FAST, "fv_f32_schemes.cu": _FAST, "fd_f32.cu": _FAST, "fv_batch_f32.cu": _FAST,
-               "fv_batch_f32_alt.cu": _FAST, "adjoint_f32.cu": _FAST, "gravity_f32.cu": _FAST}
+               "fv_batch_f32_alt.cu": _FAST, "adjoint_f32.cu": _FAST, "gravity_f32.cu": _FAST,
+               "fv_f32_split_am.cu": _FAST}
 
 
 def _nvcc():

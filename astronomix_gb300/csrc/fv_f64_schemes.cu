@@ -14,6 +14,7 @@ namespace amx {
   }
 
 bool fv_kernel_f64_schemes(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out) {
+  if (scheme == FV_SPLIT && rs == RS_AM) return fv_kernel_f64_split_am(dim, mhd, out);
   AMX_FV_SCHEME_CASE(1, RS_HLL, false, FV_SPLIT)
   AMX_FV_SCHEME_CASE(1, RS_HLLC, false, FV_SPLIT)
   AMX_FV_SCHEME_CASE(1, RS_LF, false, FV_SPLIT)

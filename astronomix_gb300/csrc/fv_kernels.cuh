@@ -814,7 +814,43 @@ __device__ __forceinline__ void sweep_tile(const FVArgs<T>& a, const int* o, con
       }
     }
     T F[NV];
-    riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), lm, F);
+    bool lmf = lm;
+    if constexpr (RS == RS_AM) {
+      // hll.py:268-326 with the sweep's input state (evolve_state.py:80-88):
+      // the compression switch of the cell right of the face, as
+      // am_compressed forms it.  Its neighbours along the sweep axis are
+      // staged; along the other axes they come from global memory through
+      // the boundary map (a reflective wall negates its axis's velocity).
+      const int hr = ((f0 + 2 * (k == 0)) * E1 + (DIM >= 2 ? f1 + 2 * (k == 1) : 0)) * E2 +
+                     (DIM >= 3 ? f2 + 2 * (k == 2) : 0);
+      const int fc[3] = {f0, f1, f2};
+      int gi[3] = {0, 0, 0};
+      bool fl_ = false;
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) gi[b] = amap(b, o[b] + fc[b], &fl_);
+      T div = T(0);
+#pragma unroll
+      for (int ax = 0; ax < DIM; ++ax) {
+        T vp, vm;
+        if (ax == k) {
+          vp = sP[(1 + ax) * HL + hr + stride];
+          vm = sP[(1 + ax) * HL + hr - stride];
+        } else {
+          bool fp = false, fm = false;
+          int ip[3] = {gi[0], gi[1], gi[2]}, im[3] = {gi[0], gi[1], gi[2]};
+          ip[ax] = amap(ax, o[ax] + fc[ax] + 1, &fp);
+          im[ax] = amap(ax, o[ax] + fc[ax] - 1, &fm);
+          vp = Pin[(1 + ax) * nc + cell_index<DIM>(ip[0], ip[1], ip[2], n)];
+          vm = Pin[(1 + ax) * nc + cell_index<DIM>(im[0], im[1], im[2], n)];
+          if (fp) vp = -vp;
+          if (fm) vm = -vm;
+        }
+        div = div + (vp - vm) / (T(2) * dxT);
+      }
+      const T c = sound_speed(sP[hr], sP[(DIM + 1) * HL + hr], gamma);
+      lmf = div < T(-0.05) * c / dxT;
+    }
+    riemann<T, DIM, RS>(qL, qR, k + 1, gamma, alpha ? alpha[k] : T(0), lmf, F, a.am == 1);
 #pragma unroll
     for (int v = 0; v < NV; ++v) sF[v * NF + f] = F[v];
   }

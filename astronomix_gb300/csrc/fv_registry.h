@@ -18,5 +18,8 @@ bool fv_kernel_f64(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out);
 // the split and VAN_ALBADA_PP instantiations (own translation units)
 bool fv_kernel_f32_schemes(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out);
 bool fv_kernel_f64_schemes(int dim, int rs, bool mhd, int scheme, FVKernelInfo* out);
+// the split sweeps with the AM_HLLC / HYBRID_HLLC switch (family 4)
+bool fv_kernel_f32_split_am(int dim, bool mhd, FVKernelInfo* out);
+bool fv_kernel_f64_split_am(int dim, bool mhd, FVKernelInfo* out);
 
 }  // namespace amx

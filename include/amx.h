@@ -49,8 +49,8 @@ extern "C" {
 #define AMX_HLLC 1
 #define AMX_HLLC_LM 2
 #define AMX_LAX_FRIEDRICHS 3
-#define AMX_HYBRID_HLLC 4  /* HLLC-LM where the cell right of a face is compressed, HLLC elsewhere (unsplit) */
-#define AMX_AM_HLLC 5      /* HYBRID_HLLC with the low-Mach dissipation control (unsplit) */
+#define AMX_HYBRID_HLLC 4  /* HLLC-LM where the cell right of a face is compressed, HLLC elsewhere */
+#define AMX_AM_HLLC 5      /* HYBRID_HLLC with the low-Mach dissipation control */
 
 #define AMX_MINMOD 0
 #define AMX_OSHER 1

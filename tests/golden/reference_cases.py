@@ -83,6 +83,15 @@ RUN_CASES = {
     "hydro2d_am_hllc": lambda: smooth_random(2, 24, seed=23, riemann=AM_HLLC, t_end=0.02, amp=0.5),
     "hydro3d_hybrid_hllc": lambda: smooth_random(3, 12, seed=24, riemann=HYBRID_HLLC, t_end=0.02, amp=0.5),
     "ot32_am_hllc": lambda: orszag_tang(n=32, t_end=0.02, riemann=AM_HLLC),
+    # the split sweeps with the compression switch (evolve_state.py:80-88 passes the sweep's state)
+    "sod_split_am_hllc": lambda: _split(sod(riemann=AM_HLLC, t_end=0.1)),
+    "hydro2d_split_hybrid_hllc": lambda: _split(smooth_random(2, 24, seed=25, riemann=HYBRID_HLLC, t_end=0.02,
+                                                              amp=0.5)),
+    "hydro2d_split_am_hllc_reflective": lambda: _split(smooth_random(2, 20, seed=27, riemann=AM_HLLC, t_end=0.02,
+                                                                     amp=0.5, boundary=REFLECTIVE_BOUNDARY)),
+    "hydro3d_split_am_hllc_open": lambda: _split(smooth_random(3, 12, seed=26, riemann=AM_HLLC, t_end=0.01, amp=0.5,
+                                                               boundary=OPEN_BOUNDARY)),
+    "ot32_split_am_hllc": lambda: _split(orszag_tang(n=32, t_end=0.02, riemann=AM_HLLC)),
     "ot32_reflective": lambda: orszag_tang(n=32, t_end=0.02, boundary=REFLECTIVE_BOUNDARY),
     "mhd2d_reflective_open": lambda: _with(smooth_random(2, 24, seed=29, mhd=True, t_end=0.01,
                                                          boundary=REFLECTIVE_BOUNDARY), boundary_settings=_mixed()),
