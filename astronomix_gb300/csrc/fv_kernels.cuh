@@ -1614,10 +1614,15 @@ fv_run_kernel(FVArgs<T> a) {
     else return rk2_unsplit(h, last);
   };
 
-  // magnetic_update (_magnetic_field_update.py:37-242); returns iterations or -1
+  // magnetic_update (_magnetic_field_update.py:37-242); returns iterations or -1.
+  // Per cell (mag_direct_cell) in 2D, and in 3D with a reflective wall, whose
+  // ghost cells of the B and v 3-vectors negate component `axis` of the wall
+  // (boundaries.py:324-355: y at x walls, z at y walls, and at z walls a
+  // fourth component, an update JAX drops); tiled or streamed otherwise.
+  const bool mag_direct = (DIM == 2) || (DIM == 3 && AxisMap<DIM>(a).reflective);
   auto magnetic = [&](T h) -> int {
     unsigned long long* slot = &ctl->mag[mag_pass % 3];
-    if (DIM == 2) {
+    if (mag_direct) {
       const MagSrc<T, DIM> first{gas + (DIM + 2) * nc, gas + nc, true};
       phase_mag_iterate_direct<T, DIM>(a, gas, first, a.mag0, h, slot, red);
     } else {
@@ -1632,7 +1637,7 @@ fv_run_kernel(FVArgs<T> a) {
     T* nxt = a.mag1;
     while (change > a.tol && it < a.max_iters) {
       slot = &ctl->mag[mag_pass % 3];
-      if (DIM == 2) {
+      if (mag_direct) {
         const MagSrc<T, DIM> src{cur, cur + 3 * nc, false};
         phase_mag_iterate_direct<T, DIM>(a, gas, src, nxt, h, slot, red);
       } else {

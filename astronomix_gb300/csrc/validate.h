@@ -58,11 +58,6 @@ inline int validate_config(const amx_config* c) {
         for (int side = 0; side < 2; ++side) {
           const int b = side ? c->bc_hi[k] : c->bc_lo[k];
           if (b != AMX_BC_OPEN && b != AMX_BC_PERIODIC && b != AMX_BC_REFLECTIVE) return AMX_ERR_UNSUPPORTED;
-          // reflective MHD: the reference fills the B and v 3-vectors by negating
-          // component `axis` (boundaries.py:324-355); reproduced in 2D.  In 3D
-          // its z wall addresses a fourth component of the 3-vectors, which is
-          // not reproduced.
-          if (c->mhd && b == AMX_BC_REFLECTIVE && c->dimensionality == 3) return AMX_ERR_UNSUPPORTED;
         }
         // periodic must be set on both sides (boundaries.py:105-111)
         if ((c->bc_lo[k] == AMX_BC_PERIODIC) != (c->bc_hi[k] == AMX_BC_PERIODIC)) return AMX_ERR_UNSUPPORTED;

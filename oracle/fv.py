@@ -52,7 +52,11 @@ def _set_along_axis(s, axis, set_index, get_index):
 
 
 def _set_var_along_axis(s, axis, set_index, get_index, var_index, factor):
-    # _geometry/boundaries.py:46-69
+    # _geometry/boundaries.py:46-69.  A var_index beyond the array's rows (the
+    # 3D z wall of the magnetic update's 3-vectors: var_index 3) is an update
+    # that JAX drops (.at[] scatters skip out-of-range indices): no change.
+    if var_index >= s.shape[0]:
+        return s
     idx_set = (var_index,) + (slice(None),) * (axis - 1) + (set_index,)
     idx_get = (var_index,) + (slice(None),) * (axis - 1) + (get_index,)
     s[idx_set] = factor * s[idx_get]

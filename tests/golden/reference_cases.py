@@ -93,6 +93,12 @@ RUN_CASES = {
                                                                boundary=OPEN_BOUNDARY)),
     "ot32_split_am_hllc": lambda: _split(orszag_tang(n=32, t_end=0.02, riemann=AM_HLLC)),
     "ot32_reflective": lambda: orszag_tang(n=32, t_end=0.02, boundary=REFLECTIVE_BOUNDARY),
+    # 3D MHD with reflective walls: the 3-vectors of the magnetic update negate
+    # y at x walls, z at y walls, and nothing at z walls (a dropped update)
+    "mhd3d_reflective": lambda: smooth_random(3, 12, seed=31, mhd=True, t_end=0.006, boundary=REFLECTIVE_BOUNDARY),
+    "mhd3d_split_reflective_open": lambda: _split(_with(smooth_random(3, 10, seed=32, mhd=True, riemann=HLLC,
+                                                                      t_end=0.006, boundary=REFLECTIVE_BOUNDARY),
+                                                        boundary_settings=_mixed())),
     "mhd2d_reflective_open": lambda: _with(smooth_random(2, 24, seed=29, mhd=True, t_end=0.01,
                                                          boundary=REFLECTIVE_BOUNDARY), boundary_settings=_mixed()),
     "fd_blast12_oblique": lambda: blast_fd(n=12, t_end=0.003, B=(0.6, 0.5, 0.4)),

@@ -147,6 +147,26 @@ def test_hydro_3d_fp32_row_staging(cuda, boundary):
         assert rel_l1(got, ref64, row=row) < 1e-5, row
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_mhd_3d_reflective(cuda, dtype):
+    """3D MHD between reflective walls: the magnetic update's ghost cells of
+    the B and v 3-vectors negate y at x walls, z at y walls and nothing at z
+    walls (boundaries.py:46-69, :324-355 under JAX's dropped out-of-range
+    update).  FP64 within 1e-12 of the oracle, FP32 within 1e-5 relative L1
+    of it, every row."""
+    cfg, prm, rv, s = smooth_random(3, 16, seed=34, mhd=True, riemann=HLLC, boundary=REFLECTIVE_BOUNDARY,
+                                    t_end=0.006, dtype=dtype)
+    got = amx.time_integration(s.copy(), cfg, prm, rv)
+    rec = {}
+    ref = odriver.time_integration(s.astype(np.float64), cfg, prm, rv, record=rec)
+    assert rec["steps"] >= 2 and sum(rec["magnetic_iterations"]) > 0
+    if dtype == np.float64:
+        assert rel_err(got, ref) < FP64_TOL
+    else:
+        for row in range(got.shape[0]):
+            assert rel_l1(got, ref, row=row) < 1e-5, row
+
+
 def test_orszag_tang_fp32_l1(cuda):
     cfg, prm, rv, s = orszag_tang(n=64, t_end=0.05, dtype=np.float32)
     got = amx.time_integration(s.copy(), cfg, prm, rv)
