@@ -47,12 +47,13 @@ WORKLOAD = ("3D MHD blast, FD 5th-order WENO + constrained transport, SSPRK(5,4)
 OT_WORKLOAD = "Orszag-Tang 2D MHD, FV HLL + Pang-Wu split (constrained B), MINMOD, SSP-RK2, 512x512 periodic, gamma 5/3"
 
 
-def workload_config(n):
+def workload_config(n, world=1):
     """The `config` of the JSON line, identical in both arms."""
     return {"workload": WORKLOAD.replace("256^3", "%d^3" % n), "grid": [n, n, n],
             "precision": "fp32 fields, fp64 dt/time/conservation sums",
             "l2": "not flushed: state 738 MB + workspace 3.4 GB per step, far above the 129 MB L2" if n >= 128
-            else "state below the L2 size"}
+            else "state below the L2 size",
+            "parallelism": "replicas" if world > 1 else "single"}
 
 
 def parse():
@@ -689,7 +690,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(args.n),
+        "config": workload_config(args.n, world),
         "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": threads, "kind": "port",
                          "sample": "compiled restatement of the reference's FD step, %d OpenMP threads, blast %d^3 "
                                    "FP32, %d steps in %.1f s (after one warm-up step)" % (threads, m, steps, dt)},
@@ -1040,8 +1041,7 @@ def run_ours(args, rank, world):
         if "fv_lf_blast_fp32" in arena:
             cfg_, prm_, rv_, s_ = arena_blast(64, "fv")
             arena["fv_lf_blast_fp32"]["cpu_baseline"] = cpu_fv_sample(cfg_, prm_, s_, 8.0)
-    config = workload_config(n)
-    config["parallelism"] = "replicas" if world > 1 else "single"
+    config = workload_config(n, world)
     line = {
         "metric": METRIC,
         "value": value,
