@@ -93,6 +93,21 @@ def test_fd_fp32_l1(cuda):
     assert rel_l1(got, ref64) < 1e-5
 
 
+def test_fd_blast_configuration_fp32_vs_fp64_to_t_end(cuda):
+    """The FD blast configuration (rho 1, p 10 inside r < 0.1 and 0.1 outside,
+    B = (1, 1, 0)/sqrt2, SSPRK(5,4), C_cfl 1.5) run to its t_end = 0.02 at
+    128^3 in FP32 and in FP64 (the FP64 kernels are held to the reference's
+    own results elsewhere): the same step count and a relative L1 density
+    difference below 1e-5 (the 256^3 run of bench.py: 9.8e-7)."""
+    res = {}
+    for dt in (np.float32, np.float64):
+        cfg, prm, rv, s = blast_fd(n=128, dtype=dt, t_end=0.02)
+        res[dt] = amx.time_integration(s.astype(dt), cfg, prm, rv)
+    assert res[np.float32].dtype == np.float32
+    assert np.isfinite(res[np.float32]).all()
+    assert rel_l1(res[np.float32], res[np.float64], row=0) < 1e-5
+
+
 def test_fd_divergence_free_at_roundoff(cuda):
     cfg, prm, rv, s = blast_fd(n=32, t_end=0.004)
     got = amx.time_integration(s.copy(), cfg, prm, rv)
