@@ -262,7 +262,7 @@ struct GravPlan {
   double dx = 1.0;
   int version = AMX_DONOR_ACCOUNTING;
   int rs = AMX_HLL;
-  int lm = 0, split = 0, first_order = 0, limiter = AMX_MINMOD;
+  int lm = 0, am = 0, split = 0, first_order = 0, limiter = AMX_MINMOD;
   long long ncells = 0;
   int num_sms = 1;
   cufftHandle fwd = 0, inv = 0;
@@ -488,6 +488,7 @@ int apply_t(GravPlan* p, const T* old, T* state, const FVControl* ctl, double dt
   a.gamma = prm.gamma;
   a.version = p->version;
   a.lm = p->lm;
+  a.am = p->am;
   a.split = p->split;
   a.first_order = p->first_order;
   a.limiter = p->limiter;
@@ -519,6 +520,7 @@ int grav_plan_create(const amx_config& c, GravPlan** out) {
   p->version = c.self_gravity_version;
   p->rs = c.riemann_solver;
   p->lm = c.riemann_solver == AMX_HLLC_LM;
+  p->am = (c.riemann_solver == AMX_AM_HLLC) ? 1 : (c.riemann_solver == AMX_HYBRID_HLLC ? 2 : 0);
   p->split = c.split;
   p->first_order = c.first_order_fallback;
   p->limiter = c.limiter;

@@ -43,6 +43,7 @@ struct GravSrc {
   double gamma;
   int version;
   int lm;
+  int am;  // AM_HLLC (1) / HYBRID_HLLC (2): the compression switch of the flux; 0 otherwise
   int split;
   int first_order;
   int limiter;
@@ -78,6 +79,48 @@ __device__ __forceinline__ void grav_load(const GravSrc<T>& a, const int* ic, in
 #pragma unroll
   for (int v = 0; v < DIM + 2; ++v) q[v] = a.old[v * a.nc + c];
   if (flip) q[k + 1] = -q[k + 1];
+}
+
+// The AM_HLLC / HYBRID_HLLC compression switch (hll.py:268-326, as
+// am_compressed forms it) of the old state's cell whose coordinate along
+// axis k is j: qm, q0, qp are its cells j - 1, j, j + 1 along k (as grav_load
+// maps them); the neighbours along the other axes come from global memory,
+// mapped the same way (a reflective wall negates its axis's velocity).
+template <typename T, int DIM>
+__device__ __forceinline__ bool grav_am_switch(const GravSrc<T>& a, const int* ic, int k, int j, const T* qm,
+                                               const T* q0, const T* qp, T gamma, T dxT) {
+  const int n = a.g.n;
+  bool fk = false;
+  int base[3] = {ic[0], ic[1], ic[2]};
+  base[k] = a.g.roll ? wrap(j, n) : map_index(j, n, a.g.bc[k], DIM == 1, &fk);
+  T div = T(0);
+#pragma unroll
+  for (int ax = 0; ax < DIM; ++ax) {
+    T vp, vm;
+    if (ax == k) {
+      vp = qp[ax + 1];
+      vm = qm[ax + 1];
+    } else {
+      T v2[2];
+#pragma unroll
+      for (int sgn = 0; sgn < 2; ++sgn) {
+        int jc[3] = {base[0], base[1], base[2]};
+        bool f = false;
+        const int g = ic[ax] + (sgn ? -1 : 1);
+        jc[ax] = a.g.roll ? wrap(g, n) : map_index(g, n, a.g.bc[ax], DIM == 1, &f);
+        long long c = jc[0];
+        if (DIM >= 2) c = c * n + jc[1];
+        if (DIM >= 3) c = c * n + jc[2];
+        const T v = a.old[(ax + 1) * a.nc + c];
+        v2[sgn] = f ? -v : v;
+      }
+      vp = v2[0];
+      vm = v2[1];
+    }
+    div = div + (vp - vm) / (T(2) * dxT);
+  }
+  const T c = sound_speed(q0[0], q0[DIM + 1], gamma);
+  return div < T(-0.05) * c / dxT;
 }
 
 // The two interface states of the centre cell q0 along axis k (left face
@@ -204,7 +247,9 @@ __global__ void __launch_bounds__(kGThreads) k_grav_faces(GravSrc<T> a) {
         riemann_split_mass<T, DIM>(hiL, lo, k + 1, gamma, lm, unstable, &to_im1, &im1);
       } else {
         T F[NV];
-        riemann<T, DIM, RS>(hiL, lo, k + 1, gamma, alpha, lm, F);
+        bool lmf = lm;
+        if constexpr (RS == RS_AM) lmf = grav_am_switch<T, DIM>(a, ic, k, j, w1, w2, w3, gamma, dxT);
+        riemann<T, DIM, RS>(hiL, lo, k + 1, gamma, alpha, lmf, F, a.am == 1);
         if (version == AMX_DONOR_ACCOUNTING) {
           to_im1 = jmin(F[0], T(0));
           im1 = jmax(F[0], T(0));
@@ -293,7 +338,9 @@ __global__ void __launch_bounds__(kGThreads) k_grav_faces_last(GravSrc<T> a) {
         riemann_split_mass<T, DIM>(hiL, lo, k + 1, gamma, lm, unstable, &to_im1, &im1);
       } else {
         T F[NV];
-        riemann<T, DIM, RS>(hiL, lo, k + 1, gamma, alpha, lm, F);
+        bool lmf = lm;
+        if constexpr (RS == RS_AM) lmf = grav_am_switch<T, DIM>(a, ic, k, j, qm, q0, qp, gamma, dxT);
+        riemann<T, DIM, RS>(hiL, lo, k + 1, gamma, alpha, lmf, F, a.am == 1);
         if (version == AMX_DONOR_ACCOUNTING) {
           to_im1 = jmin(F[0], T(0));
           im1 = jmax(F[0], T(0));
@@ -386,12 +433,14 @@ void grav_faces_axis(const GravSrc<T>& a, int rs, int num_sms, cudaStream_t s) {
     const int grid = grav_grid_for(warps * 32, num_sms);
     if (rs == AMX_LAX_FRIEDRICHS) k_grav_faces_last<T, DIM, RS_LF><<<grid, kGThreads, 0, s>>>(a);
     else if (rs == AMX_HLL) k_grav_faces_last<T, DIM, RS_HLL><<<grid, kGThreads, 0, s>>>(a);
+    else if (a.am) k_grav_faces_last<T, DIM, RS_AM><<<grid, kGThreads, 0, s>>>(a);
     else k_grav_faces_last<T, DIM, RS_HLLC><<<grid, kGThreads, 0, s>>>(a);
     return;
   }
   const int grid = grav_grid_for(ntrans * ((a.g.n + kGSeg - 1) / kGSeg), num_sms);
   if (rs == AMX_LAX_FRIEDRICHS) k_grav_faces<T, DIM, RS_LF, K><<<grid, kGThreads, 0, s>>>(a);
   else if (rs == AMX_HLL) k_grav_faces<T, DIM, RS_HLL, K><<<grid, kGThreads, 0, s>>>(a);
+  else if (a.am) k_grav_faces<T, DIM, RS_AM, K><<<grid, kGThreads, 0, s>>>(a);
   else k_grav_faces<T, DIM, RS_HLLC, K><<<grid, kGThreads, 0, s>>>(a);
 }
 

@@ -29,10 +29,6 @@ inline int validate_config(const amx_config* c) {
     if (c->mhd && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
     if (c->split != 0 && c->split != 1) return AMX_ERR_INVALID_ARG;
     if (c->riemann_solver < AMX_HLL || c->riemann_solver > AMX_AM_HLLC) return AMX_ERR_UNSUPPORTED;
-    // AM_HLLC / HYBRID_HLLC: unsplit and split schemes; the self-gravity
-    // source term's fluxes have no compression switch here
-    const bool am = c->riemann_solver == AMX_HYBRID_HLLC || c->riemann_solver == AMX_AM_HLLC;
-    if (am && c->self_gravity) return AMX_ERR_UNSUPPORTED;
     if (c->limiter < AMX_MINMOD || c->limiter > AMX_VAN_ALBADA_PP) return AMX_ERR_UNSUPPORTED;
     // the reference's 1D VAN_ALBADA_PP sums its velocity terms over the whole grid
     if (c->limiter == AMX_VAN_ALBADA_PP && !c->split && c->dimensionality < 2) return AMX_ERR_UNSUPPORTED;
