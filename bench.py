@@ -62,7 +62,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=N_CELLS)
+    ap.add_argument("--n", type=int, default=None,
+                    help="cells per axis (default: %d for the headline; each --case has its own)" % N_CELLS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-arena", action="store_true", help="skip the 256^3 blast comparison")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the 64-run batched ensemble")
@@ -80,7 +81,7 @@ def parse():
 
 def run_case(name, n=None):
     """Small, self-contained runs of the workloads for ncu captures:
-    fdblast: the headline FD blast at --n^3 FP32, 2 steps (one warm-up);
+    fdblast: the headline FD blast at --n^3 (default 256^3) FP32, 2 steps (one warm-up);
     fd: the reference's FD WENO-CT arena blast 128^3 FP32, 2 steps; fv3d: FV Lax-Friedrichs MHD
     blast (--n, default 192)^3 FP32, 2 steps (one launch); fv3dseams: the same blast, the RK2 hydro
     seam and the magnetic seam called twice each (four launches; ncu -s 2 -c 2 takes the second
@@ -99,6 +100,7 @@ def run_case(name, n=None):
         from _cases import blast_fd
         from astronomix_gb300.time_integration import get_plan
 
+        n = n or N_CELLS
         cfg, prm, rv, s = blast_fd(n=n, dtype=np.float32, t_end=1e9)
         plan = get_plan(cfg, rv, s.shape, np.float32)
         dev = torch.from_numpy(s.astype(np.float32)).cuda()
@@ -690,7 +692,7 @@ def run_reference(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "zone-updates/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, steps),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(args.n, world),
+        "config": workload_config(args.n or N_CELLS, world),
         "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": threads, "kind": "port",
                          "sample": "compiled restatement of the reference's FD step, %d OpenMP threads, blast %d^3 "
                                    "FP32, %d steps in %.1f s (after one warm-up step)" % (threads, m, steps, dt)},
@@ -945,7 +947,7 @@ def run_ours(args, rank, world):
     from astronomix_gb300.replicas import replica_throughput
 
     dev_index = torch.cuda.current_device()
-    n = args.n
+    n = args.n or N_CELLS
     cfg, prm, rv, s = blast_fd(n=n, dtype=np.float32, t_end=1e9)
     s = s.astype(np.float32)
     p = _native.make_params(prm)
