@@ -127,3 +127,30 @@ def test_oracle_fd_step():
     P = np.concatenate([ofd.prim_from_cons(U, 1e-14, 1e-14, 5 / 3), np.stack([bx, by, bz])])
     got = ofd.evolve_state_fd(P, 2e-3, 5 / 3, 1 / 8, 1e-14, 1e-14)
     assert rel_err(got, FIX["evolve_state_fd/output"]) < TOL
+
+
+def test_out_of_range_component_semantics():
+    """The reference's 3D z wall names component 3 of the magnetic update's
+    3-vectors (boundaries.py:46-69 with var_index = axis = 3).  Under JAX a
+    read at that static index clamps and the .at[] update is dropped; the
+    NumPy stand-in used for the fixtures keeps both rules, and the oracle
+    treats the update as the no-op it is."""
+    sys.path.insert(0, os.path.join(HERE, "golden", "jaxshim"))
+    try:
+        from jax._array import JArray
+    finally:
+        sys.path.pop(0)
+        for m in [m for m in sys.modules if m == "jax" or m.startswith("jax.")]:
+            del sys.modules[m]  # the stand-in stays out of the other tests
+    x = np.arange(3 * 4, dtype=np.float64).reshape(3, 4).view(JArray)
+    assert np.array_equal(np.asarray(x[3]), np.asarray(x[2]))        # read: clamped to the last row
+    assert np.array_equal(np.asarray(x[(3, slice(None))]), np.asarray(x[2]))
+    y = x.at[(3, 1)].set(-1.0)                                          # update: dropped
+    assert np.array_equal(np.asarray(y), np.asarray(x))
+    z = x.at[(1, 1)].set(-1.0)                                          # in range: applied
+    assert float(z[1, 1]) == -1.0 and float(x[1, 1]) == 5.0
+    s = np.arange(3 * 6 * 6 * 6, dtype=np.float64).reshape(3, 6, 6, 6)
+    t = ofv._set_var_along_axis(s.copy(), 3, 0, 3, 3, -1.0)             # z wall of a 3-vector
+    assert np.array_equal(t, s)
+    u = ofv._set_var_along_axis(s.copy(), 1, 0, 3, 1, -1.0)             # x wall: component y negated
+    assert np.array_equal(u[1, 0], -s[1, 3]) and np.array_equal(u[0], s[0])
